@@ -1,0 +1,423 @@
+"""Benchmark of the GB300 software ray-tracing core.
+
+Workload (one "step"): closest-hit traversal of 1920x1080 coherent primary
+rays plus 1920x1080 incoherent rays (origins uniform in the unit cube,
+directions uniform on the sphere) against a seeded soup of 1,000,000 FP32
+triangles in the unit cube (LBVH -> BVH8 built once, outside the timed
+region).  Metric: Mrays/s over both ray sets, inputs resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  Besides the headline value it reports:
+  e2e           the same metric through the C ABI with rays in pinned host
+                memory and hits copied back, copies inside the timed region
+  roofline      achieved algorithmic GB/s of the traversal kernel (rays x
+                (48 B ray I/O + 80 B x nodes visited + 36 B x triangles
+                tested), counts from the instrumented kernel) over measured
+                HBM bandwidth
+  cpu_baseline  the CPU oracle (same BVH8, same traversal, all host threads)
+                on a bounded sample of the same rays
+  shadow/build  any-hit shadow-ray Mrays/s and BVH build ms (not in value)
+  clocks        nvidia-smi samples taken during the timed region
+--impl reference times the CPU implementation (the oracle port: the
+reference's own ray tracing runs in a Vulkan driver, which does not exist on
+this machine) on the same workload and prints the same line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "build-up-phase_gb300"
+for p in (str(REPO), str(PKG)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+N_TRIS = 1_000_000
+W, H = 1920, 1080
+CAMERA = ((0.5, 0.5, 2.5), 60.0)
+LIGHT = (0.5, 2.0, 0.5)
+METRIC = "Mrays/s primary+incoherent (closest hit), 1M-triangle soup, 1920x1080 each"
+WORKLOAD = "triangle soup 1M tris (unit cube, edges U(0.001,0.02)); 1920x1080 primary + 1920x1080 incoherent rays"
+BYTES_RAY_IO = 48   # 32 B ray in + 16 B hit out
+BYTES_NODE = 80     # compressed BVH8 node
+BYTES_TRI = 36      # FP32 vertex triplet
+
+
+def _env_int(name: str, default: int) -> int:
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path("/tmp") / f"rt_bench_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def primary_rays_np():
+    """The sample's pinhole raygen for the 1920x1080 launch, in numpy float32
+    (the same op sequence as rt_generate_primary_rays)."""
+    import math
+    f32 = np.float32
+    from rtcore.scenes import RAY_DTYPE
+    half = f32(f32(f32(CAMERA[1]) * f32(math.pi / 180.0)) * f32(0.5))
+    ay = f32(math.tan(float(half)))
+    ax = f32(f32(ay * f32(W)) / f32(H))
+    ndx = ((np.arange(W, dtype=np.float32) + f32(0.5)) / f32(W)) * f32(2) - f32(1)
+    ndy = ((np.arange(H, dtype=np.float32) + f32(0.5)) / f32(H)) * f32(2) - f32(1)
+    rays = np.zeros(W * H, RAY_DTYPE)
+    d = np.empty((H, W, 3), np.float32)
+    p = (ndx * ax)[None, :]
+    q = (ndy * ay)[:, None]
+    d[..., 0] = (p * f32(1) + q * f32(0)) + f32(0)
+    d[..., 1] = (p * f32(0) + q * f32(-1)) + f32(0)
+    d[..., 2] = (p * f32(0) + q * f32(0)) + f32(-1)
+    rays["dir"] = d.reshape(-1, 3)
+    rays["org"] = np.asarray(CAMERA[0], np.float32)
+    rays["tmax"] = 100.0
+    return rays
+
+
+def workload():
+    import rtcore.scenes as S
+    seed = S.SEED_BASE + 2
+    v, i = S.soup(seed, N_TRIS)
+    prim = primary_rays_np()
+    inc = S.incoherent_rays(seed, W * H, (0, 0, 0), (1, 1, 1), 1e30)
+    return v, i, prim, inc
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port): the reference arm and the cpu_baseline leg
+# ---------------------------------------------------------------------------
+
+def cpu_trace_rate(v, i, prim, inc, n_sample: int, threads: int = 0, repeats: int = 1):
+    """Mrays/s of the oracle's BVH8 closest-hit traversal (all host threads)
+    on the first n_sample rays of each set."""
+    import oracle
+    accel, rc = oracle.build_blas([(v, i, None)])
+    rays = np.concatenate([prim[:: max(1, len(prim) // n_sample)][:n_sample],
+                           inc[:n_sample]])
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        oracle.trace_closest(accel, rays, threads)
+        times.append(time.perf_counter() - t0)
+    return len(rays) / min(times) / 1e6, len(rays), (threads or oracle.hw_threads())
+
+
+def run_reference(args) -> int:
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    import oracle
+    v, i, prim, inc = workload()
+    accel, rc = oracle.build_blas([(v, i, None)])
+    n = 250_000
+    rays = np.concatenate([prim[:: len(prim) // n][:n], inc[:n]])
+    threads = oracle.hw_threads()
+    for _ in range(args.warmup):
+        oracle.trace_closest(accel, rays[:20000], threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.trace_closest(accel, rays, threads)
+    dt = time.perf_counter() - t0
+    value = len(rays) * args.steps / dt / 1e6
+    sample = f"{n} primary (strided) + {n} incoherent rays of the workload per step"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "tris": N_TRIS, "rays_per_step": len(rays)},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's ray tracing runs inside a Vulkan driver on RT cores; no Vulkan stack exists "
+                    "on this machine, so the CPU port of the same algorithm (oracle/) is timed"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+def run_ours(args) -> int:
+    import torch
+    import rtcore
+    from rtcore.scenes import RAY_DTYPE
+    sys.path.insert(0, str(PKG))
+    import build as rt_build
+    rt_build.build()
+
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = rtcore.Context(local)
+    stream = torch.cuda.current_stream()
+
+    v, i, prim, inc = workload()
+    n_p, n_i = len(prim), len(inc)
+    n_all = n_p + n_i
+
+    # ---- scene upload + build (timed separately: build ms)
+    dv = torch.from_numpy(v.reshape(-1)).to(dev)
+    di = torch.from_numpy(i.reshape(-1).view(np.int32)).to(dev)
+    g = rtcore.GeometryTriangles()
+    g.vertices, g.vertex_stride, g.max_vertex = dv.data_ptr(), 12, len(v) - 1
+    g.index_type, g.indices, g.tri_count, g.flags = rtcore.RT_INDEX_UINT32, di.data_ptr(), N_TRIS, 1
+    sz = ctx.blas_sizes([N_TRIS])
+    accel = torch.empty(sz.accel_bytes, dtype=torch.uint8, device=dev)
+    scratch = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device=dev)
+    build_ms = []
+    for k in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.build_blas([g], 0, accel, sz.accel_bytes, scratch, sz.scratch_bytes, stream)
+        e1.record(stream)
+        ctx.sync(stream)
+        if k:
+            build_ms.append(e0.elapsed_time(e1))
+    n_nodes, _, depth = ctx.accel_info(accel, stream)
+    addr = ctx.address(accel)
+
+    # ---- rays resident in HBM
+    rays_p = torch.from_numpy(prim.view(np.uint8)).to(dev)
+    rays_i = torch.from_numpy(inc.view(np.uint8)).to(dev)
+    hits_p = torch.empty(n_p * 16, dtype=torch.uint8, device=dev)
+    hits_i = torch.empty(n_i * 16, dtype=torch.uint8, device=dev)
+
+    # ---- traversal statistics (instrumented kernel, untimed)
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+    ctx.trace_stats(addr, rays_p, n_p, False, cnt, stream)
+    ctx.sync(stream)
+    st_p = cnt.cpu().numpy().astype(float) / n_p
+    ctx.trace_stats(addr, rays_i, n_i, False, cnt, stream)
+    ctx.sync(stream)
+    st_i = cnt.cpu().numpy().astype(float) / n_i
+    bytes_p = BYTES_RAY_IO + BYTES_NODE * st_p[0] + BYTES_TRI * st_p[1]
+    bytes_i = BYTES_RAY_IO + BYTES_NODE * st_i[0] + BYTES_TRI * st_i[1]
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        ctx.trace_closest(addr, rays_p, hits_p, n_p, stream=stream)
+        if ev:
+            ev[1].record(stream)
+        ctx.trace_closest(addr, rays_i, hits_i, n_i, stream=stream)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+        flush.fill_(1)
+    ctx.sync(stream)
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            step(evs[k])
+            flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    if dist:
+        tdist.barrier()
+    ctx.sync(stream)
+    t_p = [e[0].elapsed_time(e[1]) for e in evs]
+    t_i = [e[1].elapsed_time(e[2]) for e in evs]
+    ms_step = (sum(t_p) + sum(t_i)) / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = n_all * world / (ms_step * 1e-3) / 1e6
+
+    # ---- roofline of the traversal kernel (both launches of the step)
+    peaks = _peaks()
+    alg_bytes = n_p * bytes_p + n_i * bytes_i
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "peak_source": peaks["source"],
+                "kernel": "k_trace_blas (closest hit)",
+                "bytes_per_ray": {"primary": round(bytes_p, 1), "incoherent": round(bytes_i, 1)},
+                "nodes_per_ray": {"primary": round(st_p[0], 3), "incoherent": round(st_i[0], 3)},
+                "tris_per_ray": {"primary": round(st_p[1], 3), "incoherent": round(st_i[1], 3)}}
+
+    # ---- shadow rays (any hit) toward a point light from primary hits
+    hp = hits_p.cpu().numpy().view(np.float32).reshape(-1, 4)
+    hitmask = hp[:, 1].view(np.uint32) != 0xFFFFFFFF
+    pts = prim["org"][hitmask] + hp[hitmask, 0:1] * prim["dir"][hitmask]
+    sh = np.zeros(int(hitmask.sum()), RAY_DTYPE)
+    sh["org"] = pts + np.float32(1e-4) * np.float32([0, 0, 1])
+    sh["dir"] = np.float32(LIGHT) - sh["org"]
+    sh["tmax"] = 1.0
+    rays_s = torch.from_numpy(sh.view(np.uint8)).to(dev)
+    occ = torch.empty(max(1, len(sh)), dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        ctx.trace_any(addr, rays_s, occ, len(sh), stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(5):
+        ctx.trace_any(addr, rays_s, occ, len(sh), stream)
+    e1.record(stream)
+    ctx.sync(stream)
+    shadow_mrays = len(sh) * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e6
+
+    # ---- e2e: rays from pinned host memory, hits back to host
+    hp_rays = torch.from_numpy(prim.view(np.uint8)).pin_memory()
+    hi_rays = torch.from_numpy(inc.view(np.uint8)).pin_memory()
+    hp_hits = torch.empty(n_p * 16, dtype=torch.uint8).pin_memory()
+    hi_hits = torch.empty(n_i * 16, dtype=torch.uint8).pin_memory()
+
+    def e2e_step():
+        rays_p.copy_(hp_rays, non_blocking=True)
+        rays_i.copy_(hi_rays, non_blocking=True)
+        ctx.trace_closest(addr, rays_p, hits_p, n_p, stream=stream)
+        ctx.trace_closest(addr, rays_i, hits_i, n_i, stream=stream)
+        hp_hits.copy_(hits_p, non_blocking=True)
+        hi_hits.copy_(hits_i, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    k_e2e = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k_e2e):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / k_e2e
+    e2e_value = n_all * world / (e2e_ms * 1e-3) / 1e6
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cv, cn, cores = cpu_trace_rate(v, i, prim, inc, 100_000)
+            cpu = {"value": round(cv, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                   "sample": f"{cn} rays (100000 strided primary + 100000 incoherent) of the workload, oracle BVH8 "
+                             f"traversal on {cores} host threads"}
+        out = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+               "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms_step, 4),
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded PCG32 scene and rays)",
+               "config": {"workload": WORKLOAD, "tris": N_TRIS, "rays_per_step": n_all,
+                          "parallelism": f"replicas{world}" if world > 1 else "single",
+                          "l2": "flushed between steps (256 MB write, outside the step events)",
+                          "bvh_nodes": n_nodes, "bvh_depth": depth},
+               "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",
+                       "h2d_bytes_per_step": n_all * 32, "d2h_bytes_per_step": n_all * 16},
+               "gpu_launches": 4 * args.steps,
+               "roofline": roofline,
+               "cpu_baseline": cpu,
+               "breakdown": {"primary_mrays": round(n_p * args.steps / (sum(t_p) * 1e-3) / 1e6, 2),
+                             "incoherent_mrays": round(n_i * args.steps / (sum(t_i) * 1e-3) / 1e6, 2),
+                             "shadow_anyhit_mrays": round(shadow_mrays, 2),
+                             "build_ms": round(statistics.median(build_ms), 3),
+                             "wall_s_timed_region": round(t_wall, 3)},
+               "clocks": clocks.summary()}
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if dist:
+        tdist.destroy_process_group()
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg")
+    args = ap.parse_args(argv)
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,982 @@
+// rt_build.cu -- LBVH -> compressed BVH8 builder (bottom and top level).
+//
+// Replaces vkCmdBuildAccelerationStructuresKHR (vulkan-raytraced-triangle/
+// main.cpp:788-811 for the BLAS, :920-940 for the TLAS) whose work the
+// reference leaves to the driver.  The steps the driver hides are explicit
+// kernels, all stream-ordered, with no host synchronisation:
+//
+//   prep      triangle records (geometry transform applied, as Vulkan applies
+//             transformData) or instance records + boxes + centroid bounds
+//   morton    30- or 63-bit Morton code of each box centre, fused with the
+//             digit histograms of the radix sort
+//   sort      onesweep LSD radix sort (rt_sort.cu), stable
+//   karras    binary radix tree over the sorted keys (Karras, HPG 2012),
+//             index-augmented keys for duplicates
+//   refit     bottom-up boxes + SAH leaf decisions (one atomic per node)
+//   collapse  one cooperative kernel, breadth-first level by level: greedy
+//             widening to 8 children, octant slot assignment, 8-bit child-box
+//             quantisation (Ylitie, Karras, Laine, HPG 2017), leaf records
+//             gathered into node order.  Node and record positions come from
+//             grid-wide prefix sums, so the output is deterministic and equal
+//             byte for byte to the CPU restatement of the same steps.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "rt_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace rtc {
+
+namespace {
+
+constexpr int kMaxGeoms = 256;
+constexpr int kCollapseThreads = 256;
+constexpr int kMaxCoopBlocks = 4096;
+constexpr uint32_t kNone = 0xffffffffu;
+
+struct GeomParams {
+    uint32_t n_geoms;
+    uint32_t table[kMaxGeoms + 1];
+    rt_geometry_triangles g[kMaxGeoms];
+};
+
+struct BuildLayout {
+    uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, parent, node_box, node_cost, leafable, visit, leaf_box,
+        wq, slots, counts, blk, misc, sort, total;
+};
+
+inline uint32_t node_capacity_for(uint32_t n) { return n < 2 ? 1u : n - 1u; }
+
+BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
+    BuildLayout L;
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t o = off;
+        off += align_up(bytes > 0 ? bytes : 1, 256);
+        return o;
+    };
+    uint64_t ni = n > 0 ? n - 1 : 0;
+    uint64_t cap = node_capacity_for(n);
+    L.recs = take((uint64_t)n * rec_bytes);
+    L.boxes = take((uint64_t)n * 24u);
+    L.keys0 = take((uint64_t)n * 8u);
+    L.keys1 = take((uint64_t)n * 8u);
+    L.ids0 = take((uint64_t)n * 4u);
+    L.ids1 = take((uint64_t)n * 4u);
+    L.bin = take(ni * 16u);
+    L.parent = take((ni + n) * 4u);
+    L.node_box = take(ni * 24u);
+    L.node_cost = take(ni * 4u);
+    L.leafable = take(ni);
+    L.visit = take(ni * 4u);
+    L.leaf_box = take((uint64_t)n * 24u);
+    L.wq = take(cap * 4u);
+    L.slots = take(cap * 32u);
+    L.counts = take(cap * 4u);
+    L.blk = take((uint64_t)kMaxCoopBlocks * 8u);
+    L.misc = take(256);
+    L.sort = take(sort_scratch_bytes(n, passes));
+    L.total = off;
+    return L;
+}
+
+// table_entries: n_geoms + 1 for a BLAS (its geometry table), 0 for a TLAS.
+uint64_t accel_bytes_for(uint32_t n, uint32_t rec_bytes, uint32_t table_entries) {
+    uint64_t cap = node_capacity_for(n);
+    uint64_t b = RT_ACCEL_HEADER_BYTES + cap * 80u + (uint64_t)n * rec_bytes + (uint64_t)table_entries * 4u;
+    return align_up(b, 256);
+}
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ Box load_box(const float *b, uint32_t i) {
+    Box x;
+    const float *p = b + (size_t)i * 6u;
+    x.lo[0] = __ldcg(p + 0); x.lo[1] = __ldcg(p + 1); x.lo[2] = __ldcg(p + 2);
+    x.hi[0] = __ldcg(p + 3); x.hi[1] = __ldcg(p + 4); x.hi[2] = __ldcg(p + 5);
+    return x;
+}
+__device__ __forceinline__ void store_box(float *b, uint32_t i, const Box &x) {
+    float *p = b + (size_t)i * 6u;
+    p[0] = x.lo[0]; p[1] = x.lo[1]; p[2] = x.lo[2];
+    p[3] = x.hi[0]; p[4] = x.hi[1]; p[5] = x.hi[2];
+}
+
+__device__ __forceinline__ uint64_t spread3_21(uint32_t x) {
+    uint64_t v = x & 0x1fffffu;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__device__ __forceinline__ void warp_minmax_atomic(int32_t *dst_min, int32_t *dst_max, int32_t mn, int32_t mx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mn != INT32_MAX) atomicMin(dst_min, mn);
+        if (mx != INT32_MIN) atomicMax(dst_max, mx);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Header / init
+// ---------------------------------------------------------------------------
+
+__global__ void k_init(rt_accel_header hdr, uint8_t *accel, int32_t *cbounds, GeomParams gp, uint32_t write_table) {
+    int t = threadIdx.x;
+    if (t == 0) *reinterpret_cast<rt_accel_header *>(accel) = hdr;
+    if (t < 3) { cbounds[t] = INT32_MAX; cbounds[3 + t] = INT32_MIN; }
+    if (write_table) {
+        uint32_t *tab = reinterpret_cast<uint32_t *>(accel + hdr.geom_offset);
+        for (uint32_t g = (uint32_t)t; g <= gp.n_geoms; g += blockDim.x) tab[g] = gp.table[g];
+    }
+}
+
+__global__ void k_empty_root(uint8_t *accel) {
+    rt_accel_header *h = reinterpret_cast<rt_accel_header *>(accel);
+    uint4 *node = reinterpret_cast<uint4 *>(accel + h->node_offset);
+    node[0] = make_uint4(0, 0, 0, 0);
+    node[1] = make_uint4(0, 0, 0, 0);
+    node[2] = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    node[3] = make_uint4(0xffffffffu, 0xffffffffu, 0, 0);
+    node[4] = make_uint4(0, 0, 0, 0);
+    h->node_count = 1;
+    h->depth = 1;
+    for (int a = 0; a < 4; ++a) { h->bounds_lo[a] = 0.0f; h->bounds_hi[a] = 0.0f; }
+}
+
+// ---------------------------------------------------------------------------
+// prep
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_prep_tris(const GeomParams gp, uint32_t n, uint4 *__restrict__ recs,
+                                                    float *__restrict__ boxes, int32_t *cbounds, uint32_t *err,
+                                                    uint32_t *hdr_status) {
+    uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t cmin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, cmax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    if (gi < n) {
+        // geometry g with table[g] <= gi < table[g+1]
+        uint32_t lo = 0, hi = gp.n_geoms;
+        while (hi - lo > 1u) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (gp.table[mid] <= gi) lo = mid; else hi = mid;
+        }
+        const uint32_t g = lo;
+        const rt_geometry_triangles &G = gp.g[g];
+        const uint32_t p = gi - gp.table[g];
+        float v[3][3];
+        bool ok = true;
+        for (int k = 0; k < 3; ++k) {
+            uint32_t idx = G.index_type == RT_INDEX_UINT32 ? G.indices[3u * p + (uint32_t)k] : 3u * p + (uint32_t)k;
+            if (idx > G.max_vertex) {
+                ok = false;
+                report_error(err, RT_ERR_BOUNDS, gi);
+                if (hdr_status) atomicCAS(hdr_status, 0u, (uint32_t)(-RT_ERR_BOUNDS));
+                break;
+            }
+            const float *src = reinterpret_cast<const float *>(reinterpret_cast<const uint8_t *>(G.vertices) +
+                                                               (size_t)idx * G.vertex_stride);
+            float pt[3] = {src[0], src[1], src[2]};
+            if (G.transform) {
+                const float *m = &G.transform->m[0][0];
+                float mm[12];
+#pragma unroll
+                for (int q = 0; q < 12; ++q) mm[q] = __ldg(m + q);
+                xform_point(mm, pt, v[k]);
+            } else {
+                v[k][0] = pt[0]; v[k][1] = pt[1]; v[k][2] = pt[2];
+            }
+        }
+        if (ok)
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a)
+                    if (isnan(v[k][a])) ok = false;
+        const float qnan = __int_as_float(0x7fc00000);
+        uint4 *r = recs + (size_t)gi * 3u;
+        r[0] = make_uint4(__float_as_uint(ok ? v[0][0] : qnan), __float_as_uint(ok ? v[0][1] : qnan),
+                          __float_as_uint(ok ? v[0][2] : qnan), gi);
+        r[1] = make_uint4(__float_as_uint(ok ? v[1][0] : qnan), __float_as_uint(ok ? v[1][1] : qnan),
+                          __float_as_uint(ok ? v[1][2] : qnan), g);
+        r[2] = make_uint4(__float_as_uint(ok ? v[2][0] : qnan), __float_as_uint(ok ? v[2][1] : qnan),
+                          __float_as_uint(ok ? v[2][2] : qnan), p);
+        Box b = box_empty();
+        if (ok)
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = fmn(fmn(v[0][a], v[1][a]), v[2][a]);
+                b.hi[a] = fmx(fmx(v[0][a], v[1][a]), v[2][a]);
+            }
+        store_box(boxes, gi, b);
+        if (ok)
+            for (int a = 0; a < 3; ++a) {
+                int32_t o = ford((b.lo[a] + b.hi[a]) * 0.5f);
+                cmin[a] = o;
+                cmax[a] = o;
+            }
+    }
+    for (int a = 0; a < 3; ++a) warp_minmax_atomic(&cbounds[a], &cbounds[3 + a], cmin[a], cmax[a]);
+}
+
+__device__ bool invert3x4(const float *m, float out[12]) {
+    float a = m[0], b = m[1], c = m[2];
+    float d = m[4], e = m[5], f = m[6];
+    float g = m[8], h = m[9], i = m[10];
+    float c00 = e * i - f * h, c01 = f * g - d * i, c02 = d * h - e * g;
+    float det = (a * c00 + b * c01) + c * c02;
+    if (!(det != 0.0f) || !isfinite(det)) return false;
+    float r = 1.0f / det;
+    float inv[9] = {c00 * r, (c * h - b * i) * r, (b * f - c * e) * r,
+                    c01 * r, (a * i - c * g) * r, (c * d - a * f) * r,
+                    c02 * r, (b * g - a * h) * r, (a * e - b * d) * r};
+    for (int row = 0; row < 3; ++row) {
+        for (int col = 0; col < 3; ++col) out[4 * row + col] = inv[3 * row + col];
+        out[4 * row + 3] = -((inv[3 * row + 0] * m[3] + inv[3 * row + 1] * m[7]) + inv[3 * row + 2] * m[11]);
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_prep_inst(const rt_instance *__restrict__ inst, uint32_t n,
+                                                    uint4 *__restrict__ recs, float *__restrict__ boxes,
+                                                    int32_t *cbounds) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t cmin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, cmax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    if (i < n) {
+        rt_instance I = inst[i];
+        const float *m = &I.transform.m[0][0];
+        float w2o[12];
+        bool ok = invert3x4(m, w2o);
+        if (!ok)
+            for (int q = 0; q < 12; ++q) w2o[q] = 0.0f;
+        const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(I.accel_ref);
+        Box b = box_empty();
+        if (ok && bh && bh->prim_count > 0) {
+            for (int c = 0; c < 8; ++c) {
+                float pt[3] = {(c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
+                               (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
+                               (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]};
+                float w[3];
+                xform_point(m, pt, w);
+                for (int a = 0; a < 3; ++a) { b.lo[a] = fmn(b.lo[a], w[a]); b.hi[a] = fmx(b.hi[a], w[a]); }
+            }
+        }
+        uint4 *r = recs + (size_t)i * 5u;
+        r[0] = make_uint4(__float_as_uint(w2o[0]), __float_as_uint(w2o[1]), __float_as_uint(w2o[2]),
+                          __float_as_uint(w2o[3]));
+        r[1] = make_uint4(__float_as_uint(w2o[4]), __float_as_uint(w2o[5]), __float_as_uint(w2o[6]),
+                          __float_as_uint(w2o[7]));
+        r[2] = make_uint4(__float_as_uint(w2o[8]), __float_as_uint(w2o[9]), __float_as_uint(w2o[10]),
+                          __float_as_uint(w2o[11]));
+        r[3] = make_uint4((uint32_t)(I.accel_ref & 0xffffffffu), (uint32_t)(I.accel_ref >> 32),
+                          I.custom_index_and_mask, I.sbt_offset_and_flags);
+        r[4] = make_uint4(i, 0u, 0u, 0u);
+        store_box(boxes, i, b);
+        if (!box_is_empty(b))
+            for (int a = 0; a < 3; ++a) {
+                int32_t o = ford((b.lo[a] + b.hi[a]) * 0.5f);
+                cmin[a] = o;
+                cmax[a] = o;
+            }
+    }
+    for (int a = 0; a < 3; ++a) warp_minmax_atomic(&cbounds[a], &cbounds[3 + a], cmin[a], cmax[a]);
+}
+
+// ---------------------------------------------------------------------------
+// morton (+ radix histograms)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_morton(const float *__restrict__ boxes, uint32_t n,
+                                                 const int32_t *__restrict__ cbounds, int bpa,
+                                                 uint64_t *__restrict__ keys, uint32_t *__restrict__ ids,
+                                                 uint32_t *__restrict__ hist, int passes) {
+    __shared__ uint32_t sh[8 * 256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) sh[i] = 0u;
+    __syncthreads();
+    float lo[3], scale[3];
+    const float maxq = (float)((1u << bpa) - 1u), cells = (float)(1u << bpa);
+    const bool any = cbounds[0] != INT32_MAX;
+    for (int a = 0; a < 3; ++a) {
+        float l = any ? ford_inv(cbounds[a]) : 0.0f, h = any ? ford_inv(cbounds[3 + a]) : 0.0f;
+        float ext = h - l;
+        lo[a] = l;
+        scale[a] = ext > 0.0f ? cells / ext : 0.0f;
+    }
+    const uint64_t inactive = bpa == 21 ? ((1ull << 63) - 1ull) : ((1ull << 30) - 1ull);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Box b = load_box(boxes, i);
+        uint64_t key;
+        if (box_is_empty(b)) {
+            key = inactive;
+        } else {
+            uint32_t q[3];
+            for (int a = 0; a < 3; ++a) {
+                float c = (b.lo[a] + b.hi[a]) * 0.5f;
+                float f = (c - lo[a]) * scale[a];
+                q[a] = !(f > 0.0f) ? 0u : (f >= maxq ? (uint32_t)maxq : (uint32_t)f);
+            }
+            key = spread3_21(q[0]) | (spread3_21(q[1]) << 1) | (spread3_21(q[2]) << 2);
+        }
+        keys[i] = key;
+        ids[i] = i;
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + ((key >> (8 * p)) & 0xffu)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        uint32_t c = sh[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// karras
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int kdelta(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((int)((uint32_t)i ^ (uint32_t)j));
+    return __clzll((long long)(a ^ b));
+}
+
+__global__ void __launch_bounds__(256) k_karras(const uint64_t *__restrict__ k, uint32_t n, uint4 *__restrict__ bin,
+                                                 uint32_t *__restrict__ parent) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = n;
+    if (i >= N - 1) return;
+    if (i == 0) parent[0] = kNone;
+    int d = (kdelta(k, N, i, i + 1) - kdelta(k, N, i, i - 1)) > 0 ? 1 : -1;
+    int dmin = kdelta(k, N, i, i - d);
+    int64_t lmax = 2;
+    while (kdelta(k, N, i, i + lmax * d) > dmin) lmax <<= 1;
+    int64_t l = 0;
+    for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(k, N, i, i + (l + t) * d) > dmin) l += t;
+    int64_t j = i + l * d;
+    int dnode = kdelta(k, N, i, j);
+    int64_t s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(k, N, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int64_t gamma = i + s * d + min(d, 0);
+    int64_t lo = min(i, j), hi = max(i, j);
+    uint32_t left = (lo == gamma) ? (kLeafBit | (uint32_t)gamma) : (uint32_t)gamma;
+    uint32_t right = (hi == gamma + 1) ? (kLeafBit | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+    bin[i] = make_uint4(left, right, (uint32_t)lo, (uint32_t)hi);
+    // parents: internal x at parent[x], leaf y at parent[n - 1 + y]
+    parent[(left & kLeafBit) ? (N - 1 + (left & ~kLeafBit)) : left] = (uint32_t)i;
+    parent[(right & kLeafBit) ? (N - 1 + (right & ~kLeafBit)) : right] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// refit + SAH
+// ---------------------------------------------------------------------------
+
+struct RefitArgs {
+    uint32_t n;
+    const uint32_t *ids;
+    const float *boxes;
+    const uint32_t *parent;
+    const uint4 *bin;
+    float *node_box;
+    float *node_cost;
+    uint8_t *leafable;
+    uint32_t *visit;
+    float *leaf_box;
+    uint32_t *err;
+};
+
+__global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    Box lb = load_box(a.boxes, a.ids[j]);
+    store_box(a.leaf_box, j, lb);
+    if (a.n < 2) return;
+    uint32_t p = a.parent[a.n - 1 + j];
+    // A radix tree over 2^30 keys is at most 96 levels deep (63 key bits +
+    // 32 index bits); the cap only guards against a corrupt parent chain.
+    for (int climb = 0; p != kNone; ++climb) {
+        if (climb >= 256 || p >= a.n - 1) {
+            report_error(a.err, RT_ERR_BOUNDS, 0x61000000u | j);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&a.visit[p], 1u) == 0u) return;
+        __threadfence();
+        uint4 nd = a.bin[p];
+        const bool ll = nd.x & kLeafBit, rl = nd.y & kLeafBit;
+        Box bl = ll ? load_box(a.leaf_box, nd.x & ~kLeafBit) : load_box(a.node_box, nd.x);
+        Box br = rl ? load_box(a.leaf_box, nd.y & ~kLeafBit) : load_box(a.node_box, nd.y);
+        float cl = ll ? RT_SAH_PRIM : __ldcg(a.node_cost + nd.x);
+        float cr = rl ? RT_SAH_PRIM : __ldcg(a.node_cost + nd.y);
+        Box b = box_union(bl, br);
+        float an = half_area(b);
+        float split;
+        if (an > 0.0f) {
+            float s = half_area(bl) * cl + half_area(br) * cr;
+            split = RT_SAH_NODE + s / an;
+        } else {
+            split = RT_SAH_NODE + (cl + cr);
+        }
+        uint32_t count = nd.w - nd.z + 1u;
+        float leaf = (float)count * RT_SAH_PRIM;
+        bool lf = count <= (uint32_t)RT_MAX_LEAF_PRIMS && leaf <= split;
+        store_box(a.node_box, p, b);
+        a.node_cost[p] = lf ? leaf : split;
+        a.leafable[p] = lf ? 1 : 0;
+        p = a.parent[p];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// collapse (cooperative, breadth-first)
+// ---------------------------------------------------------------------------
+
+struct CollapseArgs {
+    uint32_t n;
+    uint32_t rec_words;  // uint4 words per leaf record (3 or 5)
+    uint32_t capacity;
+    uint32_t root_ref;
+    const uint4 *recs_in;
+    uint4 *recs_out;
+    const uint32_t *ids;
+    const uint4 *bin;
+    const float *node_box;
+    const uint8_t *leafable;
+    const float *leaf_box;
+    uint32_t *wq;
+    uint32_t *slots;
+    uint32_t *counts;
+    uint32_t *blk;
+    uint4 *nodes_out;
+    rt_accel_header *hdr;
+    uint32_t *err;
+};
+
+__device__ __forceinline__ bool ref_is_leaf(uint32_t r) { return (r & kLeafBit) != 0u; }
+__device__ __forceinline__ Box ref_box(const CollapseArgs &a, uint32_t r) {
+    return ref_is_leaf(r) ? load_box(a.leaf_box, r & ~kLeafBit) : load_box(a.node_box, r);
+}
+__device__ __forceinline__ bool ref_openable(const CollapseArgs &a, uint32_t r) {
+    return !ref_is_leaf(r) && a.leafable[r] == 0;
+}
+
+__device__ int collapse_children(const CollapseArgs &a, uint32_t src, uint32_t out[8]) {
+    if (!ref_openable(a, src)) { out[0] = src; return 1; }
+    uint4 nd = a.bin[src];
+    int n = 2;
+    out[0] = nd.x;
+    out[1] = nd.y;
+    while (n < 8) {
+        int best = -1;
+        float best_a = -1.0f;
+        for (int i = 0; i < n; ++i) {
+            if (!ref_openable(a, out[i])) continue;
+            float ar = half_area(ref_box(a, out[i]));
+            if (ar > best_a) { best_a = ar; best = i; }
+        }
+        if (best < 0) break;
+        uint4 c = a.bin[out[best]];
+        out[best] = c.x;
+        out[n++] = c.y;
+    }
+    return n;
+}
+
+__device__ void assign_slots(const Box &node, const Box *cb, int n, int slot_of[8]) {
+    float diff[8][3];
+    float ncen[3];
+    const bool ne = box_is_empty(node);
+    for (int q = 0; q < 3; ++q) ncen[q] = (node.lo[q] + node.hi[q]) * 0.5f;
+    for (int c = 0; c < n; ++c)
+        for (int q = 0; q < 3; ++q)
+            diff[c][q] = (box_is_empty(cb[c]) || ne) ? 0.0f : (cb[c].lo[q] + cb[c].hi[q]) * 0.5f - ncen[q];
+    bool used[8] = {false, false, false, false, false, false, false, false};
+    for (int c = 0; c < n; ++c) slot_of[c] = -1;
+    for (int it = 0; it < n; ++it) {
+        int bc = -1, bs = -1;
+        float bv = kInf;
+        for (int c = 0; c < n; ++c) {
+            if (slot_of[c] >= 0) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (used[s]) continue;
+                float x = (s & 1) ? -diff[c][0] : diff[c][0];
+                float y = (s & 2) ? -diff[c][1] : diff[c][1];
+                float z = (s & 4) ? -diff[c][2] : diff[c][2];
+                float cost = (x + y) + z;
+                if (bc < 0 || cost < bv) { bc = c; bs = s; bv = cost; }
+            }
+        }
+        slot_of[bc] = bs;
+        used[bs] = true;
+    }
+}
+
+// Phase A: children and slots of wide node k; returns (n_int, n_prim).
+__device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, uint32_t &n_int, uint32_t &n_prim) {
+    // wq, slots and counts are written by other blocks of this launch between
+    // grid barriers: read them through L2 (__ldcg), never a stale L1 line.
+    uint32_t src = __ldcg(a.wq + k);
+    uint32_t ch[8];
+    int nc = collapse_children(a, src, ch);
+    Box cb[8];
+    for (int c = 0; c < nc; ++c) cb[c] = ref_box(a, ch[c]);
+    Box nbox = ref_box(a, src);
+    int slot_of[8];
+    assign_slots(nbox, cb, nc, slot_of);
+    uint32_t slot_ref[8] = {kNone, kNone, kNone, kNone, kNone, kNone, kNone, kNone};
+    for (int c = 0; c < nc; ++c) slot_ref[slot_of[c]] = ch[c];
+    uint32_t ni = 0, np = 0;
+    for (int s = 0; s < 8; ++s) {
+        uint32_t r = slot_ref[s];
+        a.slots[(size_t)k * 8u + s] = r;
+        if (r == kNone) continue;
+        if (ref_openable(a, r)) {
+            ++ni;
+        } else {
+            np += ref_is_leaf(r) ? 1u : (a.bin[r].w - a.bin[r].z + 1u);
+        }
+    }
+    n_int = ni;
+    n_prim = np;
+}
+
+// Phase B: writes wide node k with its child and record bases.
+__device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t child_base, uint32_t prim_base) {
+    const uint32_t src = __ldcg(a.wq + k);
+    const Box node = ref_box(a, src);
+    uint32_t slot_ref[8];
+    Box sbox[8];
+    for (int s = 0; s < 8; ++s) {
+        slot_ref[s] = __ldcg(a.slots + (size_t)k * 8u + s);
+        if (slot_ref[s] != kNone) sbox[s] = ref_box(a, slot_ref[s]);
+        else sbox[s] = box_empty();
+    }
+    const bool empty = box_is_empty(node);
+    float p[3];
+    int e[3];
+    for (int q = 0; q < 3; ++q) {
+        p[q] = empty ? 0.0f : node.lo[q];
+        e[q] = empty ? 0 : qexp_for(__fsub_ru(node.hi[q], p[q]));
+    }
+    uint8_t qlo[3][8], qhi[3][8], meta[8];
+    uint32_t imask = 0, off = 0, ichild = 0;
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t r = slot_ref[s];
+        const bool inv = (r == kNone) || empty || box_is_empty(sbox[s]);
+        for (int q = 0; q < 3; ++q) {
+            if (inv) { qlo[q][s] = 255; qhi[q][s] = 0; continue; }
+            float sc = pow2f(-e[q]);
+            float dl = __fsub_rd(sbox[s].lo[q], p[q]) * sc;
+            float dh_raw = __fsub_ru(sbox[s].hi[q], p[q]);
+            float dh = dh_raw * sc;
+            float fl = floorf(dl), fh = ceilf(dh);
+            int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
+            int qh = fh < 0.0f ? 0 : (fh > 255.0f ? 255 : (int)fh);
+            if (qh == 0 && dh_raw > 0.0f) qh = 1;
+            qlo[q][s] = (uint8_t)ql;
+            qhi[q][s] = (uint8_t)qh;
+        }
+        meta[s] = 0;
+        if (r == kNone) continue;
+        if (ref_openable(a, r)) {
+            imask |= 1u << s;
+            meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+            uint32_t dst = child_base + ichild++;
+            if (dst < a.capacity) a.wq[dst] = r;
+            else report_error(a.err, RT_ERR_BOUNDS, 0x60000000u | k);
+        } else {
+            uint32_t first, last;
+            if (ref_is_leaf(r)) { first = last = r & ~kLeafBit; }
+            else { uint4 nd = a.bin[r]; first = nd.z; last = nd.w; }
+            uint32_t cnt = last - first + 1u;
+            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | off);
+            for (uint32_t j = 0; j < cnt; ++j) {
+                const uint4 *srcr = a.recs_in + (size_t)a.ids[first + j] * a.rec_words;
+                uint4 *dstr = a.recs_out + (size_t)(prim_base + off + j) * a.rec_words;
+                for (uint32_t w = 0; w < a.rec_words; ++w) dstr[w] = srcr[w];
+            }
+            off += cnt;
+        }
+    }
+    auto pack4 = [](const uint8_t *b) {
+        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+    };
+    uint4 *o = a.nodes_out + (size_t)k * 5u;
+    uint32_t w0w = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
+                   ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
+    o[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), w0w);
+    o[1] = make_uint4(child_base, prim_base, pack4(meta), pack4(meta + 4));
+    o[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+    o[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+    o[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+}
+
+template <int N>
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *s_red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint32_t s = 0;
+    for (int i = 0; i < N / 32; ++i) s += s_red[i];
+    __syncthreads();
+    return s;
+}
+
+template <int N>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_red, uint32_t &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_red[w] = x;
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int i = 0; i < N / 32; ++i) {
+        uint32_t c = s_red[i];
+        if (i < w) before += c;
+        tot += c;
+    }
+    __syncthreads();
+    total = tot;
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ uint32_t s_red[kCollapseThreads / 32];
+    const uint32_t G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+    if (b == 0 && t == 0) a.wq[0] = a.root_ref;
+    grid.sync();
+    uint32_t level_start = 0, level_count = 1, prim_next = 0, depth = 0;
+    // Every block evaluates the same level sizes, so all leave together; the
+    // level cap (a wide tree is never deeper than its <= 96-level binary
+    // tree) only guards against corrupt inputs.
+    while (level_count > 0) {
+        if (depth >= 256 || level_start + level_count > a.capacity) {
+            if (b == 0 && t == 0) report_error(a.err, RT_ERR_BOUNDS, 0x62000000u | depth);
+            break;
+        }
+        ++depth;
+        const uint32_t chunk = (level_count + G - 1u) / G;
+        const uint32_t c0 = min(b * chunk, level_count), c1 = min(c0 + chunk, level_count);
+        uint32_t my_int = 0, my_prim = 0;
+        for (uint32_t k = c0 + t; k < c1; k += kCollapseThreads) {
+            uint32_t ni, np;
+            collapse_phase_a(a, level_start + k, ni, np);
+            a.counts[level_start + k] = ni | (np << 16);
+            my_int += ni;
+            my_prim += np;
+        }
+        my_int = block_sum<kCollapseThreads>(my_int, s_red);
+        my_prim = block_sum<kCollapseThreads>(my_prim, s_red);
+        if (t == 0) { a.blk[2 * b] = my_int; a.blk[2 * b + 1] = my_prim; }
+        grid.sync();
+        uint32_t pre_i = 0, pre_p = 0, tot_i = 0, tot_p = 0;
+        for (uint32_t q = t; q < G; q += kCollapseThreads) {
+            uint32_t vi = __ldcg(a.blk + 2 * q), vp = __ldcg(a.blk + 2 * q + 1);
+            tot_i += vi;
+            tot_p += vp;
+            if (q < b) { pre_i += vi; pre_p += vp; }
+        }
+        pre_i = block_sum<kCollapseThreads>(pre_i, s_red);
+        pre_p = block_sum<kCollapseThreads>(pre_p, s_red);
+        tot_i = block_sum<kCollapseThreads>(tot_i, s_red);
+        tot_p = block_sum<kCollapseThreads>(tot_p, s_red);
+        const uint32_t next_start = level_start + level_count;
+        uint32_t run_i = pre_i, run_p = pre_p;
+        for (uint32_t kb = c0; kb < c1; kb += kCollapseThreads) {
+            const uint32_t k = kb + t;
+            const bool valid = k < c1;
+            const uint32_t packed = valid ? __ldcg(a.counts + level_start + k) : 0u;
+            uint32_t total;
+            const uint32_t ex = block_excl_scan<kCollapseThreads>(packed, s_red, total);
+            if (valid)
+                collapse_phase_b(a, level_start + k, next_start + run_i + (ex & 0xffffu),
+                                 prim_next + run_p + (ex >> 16));
+            run_i += total & 0xffffu;
+            run_p += total >> 16;
+        }
+        level_start = next_start;
+        level_count = tot_i;
+        prim_next += tot_p;
+        grid.sync();
+    }
+    if (b == 0 && t == 0) {
+        Box rb = ref_box(a, a.root_ref);
+        a.hdr->node_count = level_start;
+        a.hdr->depth = depth;
+        for (int q = 0; q < 3; ++q) { a.hdr->bounds_lo[q] = rb.lo[q]; a.hdr->bounds_hi[q] = rb.hi[q]; }
+        a.hdr->bounds_lo[3] = 0.0f;
+        a.hdr->bounds_hi[3] = 0.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host driver shared by BLAS and TLAS
+// ---------------------------------------------------------------------------
+
+int coop_grid(rt_context *ctx) {
+    static int cached_dev = -1, cached = 0;
+    if (cached_dev == ctx->device) return cached;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, kCollapseThreads, 0) != cudaSuccess)
+        return 0;
+    int g = per_sm * ctx->sm_count;
+    if (g > kMaxCoopBlocks) g = kMaxCoopBlocks;
+    cached = g;
+    cached_dev = ctx->device;
+    return g;
+}
+
+struct BuildCall {
+    uint32_t kind;
+    uint32_t n;
+    uint32_t rec_bytes;
+    uint32_t n_geoms;
+    uint32_t flags;
+};
+
+int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomParams *gp,
+              const rt_instance *instances, void *accel, uint64_t accel_bytes, void *scratch,
+              uint64_t scratch_bytes, BuildLayout *out_layout) {
+    const int bpa = (bc.flags & RT_BUILD_MORTON30) ? 10 : 21;
+    const int passes = bpa == 10 ? 4 : 8;
+    const uint32_t n = bc.n;
+    BuildLayout L = build_layout(n, bc.rec_bytes, passes);
+    if (out_layout) *out_layout = L;
+    const uint64_t need_accel =
+        accel_bytes_for(n, bc.rec_bytes, bc.kind == RT_ACCEL_KIND_BLAS ? bc.n_geoms + 1u : 0u);
+    if (accel_bytes < need_accel) return set_error(ctx, RT_ERR_OOM, "accel buffer smaller than rt_get_*_build_sizes");
+    if (scratch_bytes < L.total) return set_error(ctx, RT_ERR_OOM, "scratch buffer smaller than rt_get_*_build_sizes");
+    if (reinterpret_cast<uintptr_t>(accel) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "accel must be 256-byte aligned");
+    if (reinterpret_cast<uintptr_t>(scratch) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "scratch must be 256-byte aligned");
+    if (n > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 2^30-1 primitives");
+
+    uint8_t *A = static_cast<uint8_t *>(accel);
+    uint8_t *S = static_cast<uint8_t *>(scratch);
+    const uint32_t cap = node_capacity_for(n);
+
+    rt_accel_header h;
+    std::memset(&h, 0, sizeof(h));
+    h.magic = RT_ACCEL_MAGIC;
+    h.version = RT_ACCEL_VERSION;
+    h.kind = bc.kind;
+    h.prim_count = n;
+    h.geom_count = bc.kind == RT_ACCEL_KIND_BLAS ? bc.n_geoms : 0u;
+    h.build_flags = bc.flags;
+    h.morton_bits = (uint32_t)bpa * 3u;
+    h.node_capacity = cap;
+    h.node_offset = RT_ACCEL_HEADER_BYTES;
+    h.prim_offset = h.node_offset + (uint64_t)cap * 80u;
+    h.geom_offset = h.prim_offset + (uint64_t)n * bc.rec_bytes;
+    h.total_bytes = need_accel;
+
+    int32_t *cb = reinterpret_cast<int32_t *>(S + L.misc);
+    static GeomParams empty_gp;  // zero-initialised; used by TLAS builds
+    k_init<<<1, 256, 0, st>>>(h, A, cb, gp ? *gp : empty_gp, gp ? 1u : 0u);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    uint32_t *hdr_status = reinterpret_cast<uint32_t *>(A) + 7;  // rt_accel_header::status
+    if (n == 0) {
+        k_empty_root<<<1, 1, 0, st>>>(A);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+        return RT_OK;
+    }
+    uint4 *recs = reinterpret_cast<uint4 *>(S + L.recs);
+    float *boxes = reinterpret_cast<float *>(S + L.boxes);
+    const unsigned nb = (n + 255u) / 256u;
+    if (bc.kind == RT_ACCEL_KIND_BLAS) {
+        k_prep_tris<<<nb, 256, 0, st>>>(*gp, n, recs, boxes, cb, ctx->d_err, hdr_status);
+    } else {
+        k_prep_inst<<<nb, 256, 0, st>>>(instances, n, recs, boxes, cb);
+    }
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+
+    uint64_t *keys0 = reinterpret_cast<uint64_t *>(S + L.keys0);
+    uint64_t *keys1 = reinterpret_cast<uint64_t *>(S + L.keys1);
+    uint32_t *ids0 = reinterpret_cast<uint32_t *>(S + L.ids0);
+    uint32_t *ids1 = reinterpret_cast<uint32_t *>(S + L.ids1);
+    void *sort_s = S + L.sort;
+    uint32_t *hist = sort_hist_ptr(sort_s);
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(hist, 0, 8u * 256u * 4u, st));
+    {
+        unsigned g = nb;
+        unsigned cap_g = (unsigned)ctx->sm_count * 8u;
+        if (g > cap_g) g = cap_g;
+        k_morton<<<g, 256, 0, st>>>(boxes, n, cb, bpa, keys0, ids0, hist, passes);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+    }
+    int sst = sort_pairs(ctx, st, keys0, ids0, keys1, ids1, n, passes, sort_s, true, ctx->d_err);
+    if (sst) return set_error(ctx, sst, "radix sort launch failed");
+
+    uint4 *bin = reinterpret_cast<uint4 *>(S + L.bin);
+    uint32_t *parent = reinterpret_cast<uint32_t *>(S + L.parent);
+    if (n >= 2) {
+        k_karras<<<(n - 1 + 255u) / 256u, 256, 0, st>>>(keys0, n, bin, parent);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+        RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.visit, 0, (size_t)(n - 1) * 4u, st));
+    }
+    RefitArgs ra;
+    ra.n = n;
+    ra.ids = ids0;
+    ra.boxes = boxes;
+    ra.parent = parent;
+    ra.bin = bin;
+    ra.node_box = reinterpret_cast<float *>(S + L.node_box);
+    ra.node_cost = reinterpret_cast<float *>(S + L.node_cost);
+    ra.leafable = reinterpret_cast<uint8_t *>(S + L.leafable);
+    ra.visit = reinterpret_cast<uint32_t *>(S + L.visit);
+    ra.leaf_box = reinterpret_cast<float *>(S + L.leaf_box);
+    ra.err = ctx->d_err;
+    k_refit<<<nb, 256, 0, st>>>(ra);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+
+    CollapseArgs ca;
+    ca.n = n;
+    ca.rec_words = bc.rec_bytes / 16u;
+    ca.capacity = cap;
+    ca.root_ref = n >= 2 ? 0u : (kLeafBit | 0u);
+    ca.recs_in = recs;
+    ca.recs_out = reinterpret_cast<uint4 *>(A + h.prim_offset);
+    ca.ids = ids0;
+    ca.bin = bin;
+    ca.node_box = ra.node_box;
+    ca.leafable = ra.leafable;
+    ca.leaf_box = ra.leaf_box;
+    ca.wq = reinterpret_cast<uint32_t *>(S + L.wq);
+    ca.slots = reinterpret_cast<uint32_t *>(S + L.slots);
+    ca.counts = reinterpret_cast<uint32_t *>(S + L.counts);
+    ca.blk = reinterpret_cast<uint32_t *>(S + L.blk);
+    ca.nodes_out = reinterpret_cast<uint4 *>(A + h.node_offset);
+    ca.hdr = reinterpret_cast<rt_accel_header *>(A);
+    ca.err = ctx->d_err;
+    int G = coop_grid(ctx);
+    if (G <= 0) return set_error(ctx, RT_ERR_CUDA, "cooperative occupancy query failed");
+    // Small levels gain nothing from a huge grid; fewer blocks make each
+    // grid barrier cheaper.
+    unsigned want = (unsigned)((cap + kCollapseThreads * 4u - 1u) / (kCollapseThreads * 4u));
+    if (want < 1u) want = 1u;
+    if ((int)want < G) G = (int)want;
+    void *args[] = {&ca};
+    RT_CUDA_CTX(ctx, cudaLaunchCooperativeKernel((const void *)k_collapse, dim3((unsigned)G),
+                                                 dim3(kCollapseThreads), args, 0, st));
+    return RT_OK;
+}
+
+}  // namespace
+}  // namespace rtc
+
+using namespace rtc;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" rt_status rt_get_blas_build_sizes(rt_context *ctx, const uint32_t *tri_counts, uint32_t n_geoms,
+                                             uint32_t flags, rt_build_sizes *out) {
+    if (!ctx || !out || (n_geoms && !tri_counts)) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_get_blas_build_sizes: null argument");
+    if (n_geoms > (uint32_t)kMaxGeoms) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 256 geometries in one BLAS");
+    uint64_t n = 0;
+    for (uint32_t g = 0; g < n_geoms; ++g) n += tri_counts[g];
+    if (n > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 2^30-1 triangles");
+    int passes = (flags & RT_BUILD_MORTON30) ? 4 : 8;
+    out->accel_bytes = accel_bytes_for((uint32_t)n, 48u, n_geoms + 1u);
+    out->scratch_bytes = build_layout((uint32_t)n, 48u, passes).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_get_tlas_build_sizes(rt_context *ctx, uint32_t n_instances, uint32_t flags,
+                                             rt_build_sizes *out) {
+    if (!ctx || !out) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_get_tlas_build_sizes: null argument");
+    if (n_instances > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "too many instances");
+    int passes = (flags & RT_BUILD_MORTON30) ? 4 : 8;
+    out->accel_bytes = accel_bytes_for(n_instances, 80u, 0);
+    out->scratch_bytes = build_layout(n_instances, 80u, passes).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_build_blas(rt_context *ctx, rt_stream stream, const rt_geometry_triangles *geoms,
+                                   uint32_t n_geoms, uint32_t flags, void *accel, uint64_t accel_bytes,
+                                   void *scratch, uint64_t scratch_bytes) {
+    if (!ctx || !accel || !scratch || (n_geoms && !geoms))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas: null argument");
+    if (n_geoms > (uint32_t)kMaxGeoms) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 256 geometries in one BLAS");
+    if ((flags & RT_BUILD_MORTON30) && (flags & RT_BUILD_MORTON63))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_MORTON30 and RT_BUILD_MORTON63 are exclusive");
+    static thread_local GeomParams gp;
+    std::memset(&gp, 0, sizeof(gp));
+    gp.n_geoms = n_geoms;
+    uint64_t total = 0;
+    for (uint32_t g = 0; g < n_geoms; ++g) {
+        const rt_geometry_triangles &G = geoms[g];
+        if (G.tri_count && (!G.vertices || G.vertex_stride < 12u ||
+                            (G.index_type != RT_INDEX_UINT32 && G.index_type != RT_INDEX_NONE) ||
+                            (G.index_type == RT_INDEX_UINT32 && !G.indices)))
+            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas: bad geometry descriptor");
+        if (G.index_type == RT_INDEX_NONE && G.tri_count && (uint64_t)G.tri_count * 3u - 1u > G.max_vertex)
+            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas: non-indexed geometry exceeds max_vertex");
+        gp.table[g] = (uint32_t)total;
+        gp.g[g] = G;
+        total += G.tri_count;
+    }
+    if (total > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 2^30-1 triangles");
+    gp.table[n_geoms] = (uint32_t)total;
+    BuildCall bc{RT_ACCEL_KIND_BLAS, (uint32_t)total, 48u, n_geoms, flags};
+    return run_build(ctx, static_cast<cudaStream_t>(stream), bc, &gp, nullptr, accel, accel_bytes, scratch,
+                     scratch_bytes, nullptr);
+}
+
+extern "C" rt_status rt_build_tlas(rt_context *ctx, rt_stream stream, const rt_instance *instances, uint32_t n,
+                                   uint32_t flags, void *accel, uint64_t accel_bytes, void *scratch,
+                                   uint64_t scratch_bytes) {
+    if (!ctx || !accel || !scratch || (n && !instances))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_tlas: null argument");
+    if ((flags & RT_BUILD_MORTON30) && (flags & RT_BUILD_MORTON63))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_MORTON30 and RT_BUILD_MORTON63 are exclusive");
+    BuildCall bc{RT_ACCEL_KIND_TLAS, n, 80u, 0u, flags};
+    return run_build(ctx, static_cast<cudaStream_t>(stream), bc, nullptr, instances, accel, accel_bytes, scratch,
+                     scratch_bytes, nullptr);
+}
+
+extern "C" uint64_t rt_accel_address(const void *accel) { return (uint64_t)(uintptr_t)accel; }
+
+extern "C" rt_status rt_accel_info(rt_context *ctx, rt_stream stream, const void *accel, uint32_t *node_count,
+                                   uint32_t *prim_count, uint32_t *tree_depth) {
+    if (!ctx || !accel) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_accel_info: null argument");
+    rt_accel_header h;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(&h, accel, sizeof(h), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
+    if (h.magic != RT_ACCEL_MAGIC) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_accel_info: not an acceleration structure");
+    if (node_count) *node_count = h.node_count;
+    if (prim_count) *prim_count = h.prim_count;
+    if (tree_depth) *tree_depth = h.depth;
+    if (h.status) return set_error(ctx, -(int)h.status, "acceleration structure build reported an error");
+    return RT_OK;
+}
+
+// Offsets (bytes from the scratch base) of the sorted Morton keys, the
+// sorted primitive ids and the binary nodes after a BLAS build, for
+// stage-by-stage comparison with the CPU restatement.
+extern "C" rt_status rt_debug_blas_scratch_layout(uint32_t n_tris, uint32_t flags, uint64_t *keys_off,
+                                                  uint64_t *ids_off, uint64_t *bin_off) {
+    int passes = (flags & RT_BUILD_MORTON30) ? 4 : 8;
+    BuildLayout L = build_layout(n_tris, 48u, passes);
+    if (keys_off) *keys_off = L.keys0;
+    if (ids_off) *ids_off = L.ids0;
+    if (bin_off) *bin_off = L.bin;
+    return RT_OK;
+}

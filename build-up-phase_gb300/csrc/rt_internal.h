@@ -1,0 +1,63 @@
+// rt_internal.h -- host-side internals shared by the translation units of
+// librtcore: the context object, error plumbing and cross-file launchers.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rtcore.h"
+#include "../../include/rtcore_accel.h"
+#include "rt_device.cuh"
+
+// Library-owned state of one device.  Replaces the Vulkan instance/device
+// bring-up of the sample (createVkInstance/createVkDevice, main.cpp:242-388).
+struct rt_context {
+    int device = 0;
+    int sm_count = 0;
+    int cc_major = 0, cc_minor = 0;
+    size_t smem_optin = 0;
+    // d_err[0]: first device-side error code (negated RT_ERR_*), d_err[1]:
+    // detail word.  Cleared by rt_sync.
+    uint32_t *d_err = nullptr;
+    // Work-stealing counters for persistent kernels, used round-robin.
+    uint32_t *d_counters = nullptr;
+    uint32_t counter_next = 0;
+    rt_trace_tuning tuning{};
+    std::string last_error;
+};
+
+namespace rtc {
+
+constexpr uint32_t kNumCounters = 256;
+
+inline uint64_t align_up(uint64_t x, uint64_t a) { return (x + a - 1u) / a * a; }
+
+// Records a host-side error on the context and returns the code.
+int set_error(rt_context *ctx, int code, const char *msg);
+int set_cuda_error(rt_context *ctx, cudaError_t e, const char *where);
+
+// Next work counter (zeroed on `stream` before it is handed out).
+uint32_t *acquire_counter(rt_context *ctx, cudaStream_t stream);
+
+// Sort (rt_sort.cu)
+uint64_t sort_scratch_bytes(uint32_t n, int passes);
+int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
+               uint32_t *vals1, uint32_t n, int passes, void *scratch, bool hist_done, uint32_t *err);
+uint32_t *sort_hist_ptr(void *scratch);
+
+}  // namespace rtc
+
+#define RT_CUDA_TRY(expr)                                  \
+    do {                                                   \
+        cudaError_t rt_e_ = (expr);                        \
+        if (rt_e_ != cudaSuccess) return RT_ERR_CUDA;      \
+    } while (0)
+
+#define RT_CUDA_CTX(ctx, expr)                                               \
+    do {                                                                     \
+        cudaError_t rt_e_ = (expr);                                          \
+        if (rt_e_ != cudaSuccess) return rtc::set_cuda_error(ctx, rt_e_, #expr); \
+    } while (0)

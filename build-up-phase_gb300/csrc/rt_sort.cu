@@ -1,0 +1,290 @@
+// rt_sort.cu -- onesweep LSD radix sort of (uint64 key, uint32 value) pairs.
+//
+// The acceleration-structure build of the reference happens inside the
+// Vulkan driver (vkCmdBuildAccelerationStructuresKHR,
+// vulkan-raytraced-triangle/main.cpp:808); its Morton-order sort is one of the
+// driver-hidden steps made explicit here.
+//
+// Algorithm: Adinets & Merrill, "Onesweep: A Faster Least Significant Digit
+// Radix Sort for GPUs" (2022).  One histogram kernel counts the 8-bit digits
+// of every pass in a single read; each pass is then one kernel in which tiles
+// rank their keys locally (warp match_any multisplit), publish per-digit
+// counts, resolve their global offsets by decoupled look-back over earlier
+// tiles, and scatter through shared memory.  Tiles are numbered in launch
+// order by an atomic counter, so a tile only waits on tiles already owned by
+// running blocks.  Every wait is bounded: on expiry the kernel records
+// RT_ERR_TIMEOUT and carries on, so the host sees an error instead of a hang.
+// The sort is stable, hence its output equals std::stable_sort by key.
+#include <cuda_runtime.h>
+
+#include "rt_internal.h"
+
+namespace rtc {
+
+namespace {
+
+constexpr int kSortThreads = 512;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRadix = 256;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagIncl = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr int kSpinLimit = 1 << 22;
+
+constexpr size_t kSortSmemBytes =
+    (size_t)kSortTile * 8u + (size_t)kSortTile * 4u + (size_t)kSortWarps * kRadix * 4u;
+
+__global__ void __launch_bounds__(256) k_sort_hist(const uint64_t *__restrict__ keys, uint32_t n, int passes,
+                                                    uint32_t *__restrict__ hist) {
+    __shared__ uint32_t sh[8][kRadix];
+    for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x) (&sh[0][0])[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 0xffu], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+        uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&hist[i], c);
+    }
+}
+
+// Exclusive scan of 256 values held one per thread by threads 0..255 of the
+// block (all threads of the block must call it).  Returns the exclusive
+// prefix for threads < 256 and writes the total to *total.
+__device__ __forceinline__ uint32_t block_scan256(uint32_t v, uint32_t *s_warp, uint32_t *total) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t x = (t < kRadix) ? v : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (t < kRadix && lane == 31) s_warp[w] = x;
+    __syncthreads();
+    if (t == 0) {
+        uint32_t s = 0;
+        for (int i = 0; i < kRadix / 32; ++i) { uint32_t c = s_warp[i]; s_warp[i] = s; s += c; }
+        s_warp[kRadix / 32] = s;
+    }
+    __syncthreads();
+    uint32_t excl = (t < kRadix) ? (x - v + s_warp[w]) : 0u;
+    if (total) *total = s_warp[kRadix / 32];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__restrict__ kin,
+                                                            const uint32_t *__restrict__ vin,
+                                                            uint64_t *__restrict__ kout,
+                                                            uint32_t *__restrict__ vout, uint32_t n, int shift,
+                                                            const uint32_t *__restrict__ hist,
+                                                            uint32_t *__restrict__ status,
+                                                            uint32_t *__restrict__ tile_counter, uint32_t *err) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + kSortTile);
+    uint32_t *s_whist = s_vals + kSortTile;  // [warp][digit]
+    __shared__ uint32_t s_digit_excl[kRadix];
+    __shared__ uint32_t s_global[kRadix];
+    __shared__ uint32_t s_warp[kRadix / 32 + 1];
+    __shared__ uint32_t s_tile;
+
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = t; i < kSortWarps * kRadix; i += kSortThreads) s_whist[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)kSortTile;
+
+    uint64_t k[kSortItems];
+    uint32_t v[kSortItems];
+    uint32_t rank[kSortItems];
+    const uint32_t wbase = base + (uint32_t)w * 32u * kSortItems;
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
+        bool valid = idx < n;
+        k[j] = valid ? kin[idx] : 0ull;
+        v[j] = valid ? vin[idx] : 0u;
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
+        bool valid = idx < n;
+        uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        uint32_t d = (uint32_t)(k[j] >> shift) & 0xffu;
+        uint32_t old = 0, below = 0;
+        int leader = lane;
+        if (valid) {
+            uint32_t peers = __match_any_sync(vmask, d);
+            leader = __ffs(peers) - 1;
+            below = __popc(peers & lt);
+            if (lane == leader) {
+                old = s_whist[w * kRadix + d];
+                s_whist[w * kRadix + d] = old + (uint32_t)__popc(peers);
+            }
+        }
+        __syncwarp();
+        old = __shfl_sync(0xffffffffu, old, leader);
+        rank[j] = old + below;
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // per digit: exclusive over warps, block total
+    uint32_t total = 0;
+    if (t < kRadix) {
+        uint32_t s = 0;
+        for (int ww = 0; ww < kSortWarps; ++ww) {
+            uint32_t c = s_whist[ww * kRadix + t];
+            s_whist[ww * kRadix + t] = s;
+            s += c;
+        }
+        total = s;
+    }
+    uint32_t dex = block_scan256(total, s_warp, nullptr);
+    uint32_t gex = block_scan256(t < kRadix ? hist[t] : 0u, s_warp, nullptr);
+    if (t < kRadix) {
+        s_digit_excl[t] = dex;
+        volatile uint32_t *st = status;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st[t] = kFlagIncl | total;
+        } else {
+            st[(size_t)tile * kRadix + t] = kFlagAgg | total;
+            __threadfence();
+            int64_t p = (int64_t)tile - 1;
+            while (p >= 0) {
+                uint32_t s;
+                int spins = 0;
+                do {
+                    s = st[(size_t)p * kRadix + t];
+                } while ((s & ~kValueMask) == 0u && ++spins < kSpinLimit);
+                if ((s & ~kValueMask) == 0u) {
+                    report_error(err, RT_ERR_TIMEOUT, 0x50000000u | (uint32_t)tile);
+                    break;
+                }
+                prefix += s & kValueMask;
+                if ((s & ~kValueMask) == kFlagIncl) break;
+                --p;
+            }
+            st[(size_t)tile * kRadix + t] = kFlagIncl | ((prefix + total) & kValueMask);
+        }
+        s_global[t] = gex + prefix;
+    }
+    __syncthreads();
+
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
+        if (idx < n) {
+            uint32_t d = (uint32_t)(k[j] >> shift) & 0xffu;
+            uint32_t pos = s_digit_excl[d] + s_whist[w * kRadix + d] + rank[j];
+            s_keys[pos] = k[j];
+            s_vals[pos] = v[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = (n - base) < (uint32_t)kSortTile ? (n - base) : (uint32_t)kSortTile;
+    for (uint32_t i = (uint32_t)t; i < tile_n; i += kSortThreads) {
+        uint64_t key = s_keys[i];
+        uint32_t d = (uint32_t)(key >> shift) & 0xffu;
+        uint32_t o = s_global[d] + (i - s_digit_excl[d]);
+        if (o < n) {
+            kout[o] = key;
+            vout[o] = s_vals[i];
+        } else {
+            report_error(err, RT_ERR_BOUNDS, 0x51000000u | (uint32_t)tile);
+        }
+    }
+}
+
+}  // namespace
+
+uint64_t sort_scratch_bytes(uint32_t n, int passes) {
+    uint64_t tiles = ((uint64_t)n + kSortTile - 1) / kSortTile;
+    if (tiles == 0) tiles = 1;
+    // histograms (8 x 256) + tile counters (8) + status (passes x tiles x 256)
+    return align_up(8u * kRadix * 4u, 256) + align_up(8u * 4u, 256) +
+           align_up((uint64_t)passes * tiles * kRadix * 4u, 256);
+}
+
+// Sorts (keys0, vals0) on the low 8*passes key bits, using (keys1, vals1) as
+// the ping-pong buffer.  After an even number of passes the result is back in
+// keys0/vals0.  `keys_hist_done`: the caller already accumulated the digit
+// histograms into the scratch (fused with key generation).
+int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
+               uint32_t *vals1, uint32_t n, int passes, void *scratch, bool hist_done, uint32_t *err) {
+    if (n == 0) return RT_OK;
+    if (n > kValueMask) return RT_ERR_UNSUPPORTED;
+    uint8_t *s = static_cast<uint8_t *>(scratch);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(s);
+    uint32_t *counters = reinterpret_cast<uint32_t *>(s + align_up(8u * kRadix * 4u, 256));
+    uint32_t *status = reinterpret_cast<uint32_t *>(s + align_up(8u * kRadix * 4u, 256) + align_up(8u * 4u, 256));
+    uint64_t tiles = ((uint64_t)n + kSortTile - 1) / kSortTile;
+    // counters and status must start at zero; the histogram too unless the
+    // caller filled it.
+    if (!hist_done) {
+        RT_CUDA_TRY(cudaMemsetAsync(hist, 0, 8u * kRadix * 4u, stream));
+        int blocks = (int)((n + 255u) / 256u);
+        int cap = ctx->sm_count * 8;
+        if (blocks > cap) blocks = cap;
+        k_sort_hist<<<blocks, 256, 0, stream>>>(keys0, n, passes, hist);
+        RT_CUDA_TRY(cudaGetLastError());
+    }
+    RT_CUDA_TRY(cudaMemsetAsync(counters, 0, 8u * 4u, stream));
+    RT_CUDA_TRY(cudaMemsetAsync(status, 0, (size_t)passes * tiles * kRadix * 4u, stream));
+    RT_CUDA_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSortSmemBytes));
+    for (int p = 0; p < passes; ++p) {
+        const uint64_t *ki = (p & 1) ? keys1 : keys0;
+        const uint32_t *vi = (p & 1) ? vals1 : vals0;
+        uint64_t *ko = (p & 1) ? keys0 : keys1;
+        uint32_t *vo = (p & 1) ? vals0 : vals1;
+        k_onesweep<<<(unsigned)tiles, kSortThreads, kSortSmemBytes, stream>>>(
+            ki, vi, ko, vo, n, 8 * p, hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err);
+        RT_CUDA_TRY(cudaGetLastError());
+    }
+    if (passes & 1) {
+        RT_CUDA_TRY(cudaMemcpyAsync(keys0, keys1, (size_t)n * 8u, cudaMemcpyDeviceToDevice, stream));
+        RT_CUDA_TRY(cudaMemcpyAsync(vals0, vals1, (size_t)n * 4u, cudaMemcpyDeviceToDevice, stream));
+    }
+    return RT_OK;
+}
+
+uint32_t *sort_hist_ptr(void *scratch) { return static_cast<uint32_t *>(scratch); }
+
+}  // namespace rtc
+
+// ---------------------------------------------------------------------------
+// C ABI: standalone pair sort (used for ray reordering and tested on its own)
+// ---------------------------------------------------------------------------
+extern "C" rt_status rt_get_sort_scratch_bytes(uint32_t n, uint32_t key_bits, uint64_t *out) {
+    if (!out || key_bits == 0 || key_bits > 64) return RT_ERR_INVALID_ARG;
+    int passes = (int)((key_bits + 7u) / 8u);
+    *out = rtc::align_up((uint64_t)n * 12u, 256) + rtc::sort_scratch_bytes(n, passes);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_sort_pairs(rt_context *ctx, rt_stream stream, uint64_t *keys, uint32_t *vals, uint32_t n,
+                                   uint32_t key_bits, void *scratch, uint64_t scratch_bytes) {
+    if (!ctx || (n && (!keys || !vals || !scratch)) || key_bits == 0 || key_bits > 64)
+        return rtc::set_error(ctx, RT_ERR_INVALID_ARG, "rt_sort_pairs: bad argument");
+    uint64_t need = 0;
+    rt_get_sort_scratch_bytes(n, key_bits, &need);
+    if (scratch_bytes < need) return rtc::set_error(ctx, RT_ERR_OOM, "rt_sort_pairs: scratch too small");
+    int passes = (int)((key_bits + 7u) / 8u);
+    uint8_t *s = static_cast<uint8_t *>(scratch);
+    uint64_t *k1 = reinterpret_cast<uint64_t *>(s);
+    uint32_t *v1 = reinterpret_cast<uint32_t *>(s + (size_t)n * 8u);
+    void *sort_s = s + rtc::align_up((uint64_t)n * 12u, 256);
+    int st = rtc::sort_pairs(ctx, static_cast<cudaStream_t>(stream), keys, vals, k1, v1, n, passes, sort_s, false,
+                             ctx->d_err);
+    if (st) return rtc::set_error(ctx, st, "rt_sort_pairs: launch failed");
+    return RT_OK;
+}

@@ -1,0 +1,691 @@
+// rt_trace.cu -- BVH8 traversal kernels and the ray-tracing pipeline.
+//
+// Replaces traceRayEXT / vkCmdTraceRaysKHR of the reference sample
+// (vulkan-raytraced-triangle/main.cpp:1047-1052 and :1349-1355), which run on
+// RT cores inside the driver.  The GB300 has no RT cores, so traversal runs
+// on the SMs:
+//
+//   k_trace_blas    persistent warps over a ray array.  A warp refills its
+//                   idle lanes from a global counter (atomic work stealing)
+//                   whenever enough of them have finished; each lane walks
+//                   the compressed BVH8 with 16-byte node loads and keeps its
+//                   traversal stack in a shared-memory ring whose bottom
+//                   spills to local memory.
+//                   Two-level structures (instances) take a per-thread path
+//                   in the same kernel, chosen on the device from the header.
+//   k_pipeline      the sample's raygen + traceRayEXT + closest-hit / miss +
+//                   imageStore, one thread per launch id.
+//
+// Visiting order (identical in the CPU restatement, so hits and statistics
+// agree exactly): a node's leaf records first, in ascending record order,
+// then its internal children in ascending (slot ^ ray octant); remaining
+// siblings are pushed as one group.  Closest hit = smallest t, ties broken by
+// the smallest (instance, triangle) key.
+#include <cmath>
+#include <cuda_runtime.h>
+
+#include "rt_internal.h"
+
+namespace rtc {
+
+namespace {
+
+constexpr int kTraceThreads = 128;
+constexpr int kRing = 16;      // shared-memory stack entries per thread
+constexpr int kMaxDepth = 64;  // total stack entries per thread
+constexpr uint32_t kNone = 0xffffffffu;
+
+struct Hit {
+    float t, u, v;
+    uint32_t rec;     // leaf-record index of the best triangle
+    uint32_t tri;     // build-input triangle index
+    uint32_t inst;    // instance index (0 for a bare BLAS)
+    bool found;
+};
+
+__device__ __forceinline__ uint4 ldg4(const uint4 *p) { return __ldg(p); }
+
+__device__ __forceinline__ bool key_less(float t, uint64_t key, float bt, uint64_t bkey) {
+    return t < bt || (t == bt && key < bkey);
+}
+
+// ---------------------------------------------------------------------------
+// Simple per-thread traversal (local-memory stack): two-level and pipeline
+// paths.  Same visiting order as the persistent kernel.
+// ---------------------------------------------------------------------------
+
+struct LocalStack {
+    uint2 e[kMaxDepth];
+    int sp;
+};
+
+template <bool ANY>
+__device__ bool traverse_blas_simple(const uint8_t *accel, const Ray &r, float tmin, Hit &h, uint64_t &hkey,
+                                     uint32_t inst, uint32_t *err, unsigned long long *stats) {
+    const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(accel);
+    if (hd->prim_count == 0) return false;
+    const uint4 *nodes = reinterpret_cast<const uint4 *>(accel + hd->node_offset);
+    const uint4 *prims = reinterpret_cast<const uint4 *>(accel + hd->prim_offset);
+    LocalStack st;
+    st.sp = 0;
+    uint32_t node = 0;
+    // A tree walk visits each node at most once; more visits (or a node
+    // index past the end) can only come from a corrupt structure.
+    const uint32_t max_visits = hd->node_count;
+    for (uint32_t visits = 0;; ++visits) {
+        if (visits >= max_visits || node >= max_visits) {
+            report_error(err, RT_ERR_BOUNDS, 0x74000000u | node);
+            return h.found;
+        }
+        NodeWords nd = load_node(nodes, node);
+        uint32_t nh, ph;
+        isect_node(r, nd, tmin, h.t, nh, ph);
+        if (stats) stats[0]++;
+        const uint32_t pbase = nd.w1.y;
+        while (ph) {
+            uint32_t i = __ffs(ph) - 1;
+            ph &= ph - 1u;
+            const uint4 *rec = prims + (size_t)(pbase + i) * 3u;
+            uint4 a = ldg4(rec), b = ldg4(rec + 1), c = ldg4(rec + 2);
+            if (stats) stats[1]++;
+            float t, u, v;
+            if (!isect_tri(r, make_float4(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), 0.f),
+                           make_float4(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z), 0.f),
+                           make_float4(__uint_as_float(c.x), __uint_as_float(c.y), __uint_as_float(c.z), 0.f),
+                           tmin, h.t, t, u, v))
+                continue;
+            uint64_t key = ((uint64_t)inst << 32) | a.w;
+            if (ANY) {
+                h.t = t; h.u = u; h.v = v; h.rec = pbase + i; h.tri = a.w; h.inst = inst; h.found = true;
+                return true;
+            }
+            if (key_less(t, key, h.t, hkey)) {
+                h.t = t; h.u = u; h.v = v; h.rec = pbase + i; h.tri = a.w; h.inst = inst; h.found = true;
+                hkey = key;
+            }
+        }
+        uint2 g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
+        for (;;) {
+            if (g.y & 0xffu) {
+                uint32_t k = __ffs(g.y & 0xffu) - 1;
+                g.y &= ~(1u << k);
+                uint32_t s = k ^ r.oct;
+                node = g.x + __popc((g.y >> 8) & ((1u << s) - 1u));
+                if (g.y & 0xffu) {
+                    if (st.sp >= kMaxDepth) {
+                        report_error(err, RT_ERR_BOUNDS, 0x70000000u);
+                        return h.found;
+                    }
+                    st.e[st.sp++] = g;
+                }
+                break;
+            }
+            if (st.sp == 0) return false;
+            g = st.e[--st.sp];
+        }
+    }
+}
+
+struct InstRec {
+    float w2o[12];
+    uint64_t accel_ref;
+    uint32_t cim, sof, id;
+};
+
+__device__ __forceinline__ InstRec load_inst(const uint4 *prims, uint32_t i) {
+    const uint4 *p = prims + (size_t)i * 5u;
+    uint4 a = ldg4(p), b = ldg4(p + 1), c = ldg4(p + 2), d = ldg4(p + 3), e = ldg4(p + 4);
+    InstRec r;
+    r.w2o[0] = __uint_as_float(a.x); r.w2o[1] = __uint_as_float(a.y); r.w2o[2] = __uint_as_float(a.z);
+    r.w2o[3] = __uint_as_float(a.w); r.w2o[4] = __uint_as_float(b.x); r.w2o[5] = __uint_as_float(b.y);
+    r.w2o[6] = __uint_as_float(b.z); r.w2o[7] = __uint_as_float(b.w); r.w2o[8] = __uint_as_float(c.x);
+    r.w2o[9] = __uint_as_float(c.y); r.w2o[10] = __uint_as_float(c.z); r.w2o[11] = __uint_as_float(c.w);
+    r.accel_ref = (uint64_t)d.x | ((uint64_t)d.y << 32);
+    r.cim = d.z;
+    r.sof = d.w;
+    r.id = e.x;
+    return r;
+}
+
+struct HitIds {
+    uint32_t custom, sbt_off, geom, prim;
+};
+
+// Full closest/any traversal of a top- or bottom-level structure.
+template <bool ANY>
+__device__ bool trace_ray(const uint8_t *accel, const float o[3], const float d[3], float tmin, float tmax,
+                          uint32_t cull_mask, Hit &h, HitIds &ids, uint32_t *err, unsigned long long *stats) {
+    const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(accel);
+    h.t = tmax; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.inst = 0; h.found = false;
+    ids.custom = 0; ids.sbt_off = 0; ids.geom = 0; ids.prim = 0;
+    uint64_t hkey = ~0ull;
+    Ray r;
+    ray_setup(r, o, d);
+    const uint8_t *hit_blas = accel;
+    if (hd->kind == RT_ACCEL_KIND_BLAS) {
+        bool any = traverse_blas_simple<ANY>(accel, r, tmin, h, hkey, 0u, err, stats);
+        if (h.found) {
+            const uint4 *prims = reinterpret_cast<const uint4 *>(accel + hd->prim_offset);
+            ids.geom = ldg4(prims + (size_t)h.rec * 3u + 1).w;
+            ids.prim = ldg4(prims + (size_t)h.rec * 3u + 2).w;
+        }
+        return ANY ? any : h.found;
+    }
+    if (hd->prim_count == 0) return false;
+    const uint4 *nodes = reinterpret_cast<const uint4 *>(accel + hd->node_offset);
+    const uint4 *prims = reinterpret_cast<const uint4 *>(accel + hd->prim_offset);
+    LocalStack st;
+    st.sp = 0;
+    uint32_t node = 0;
+    bool done = false;
+    for (uint32_t visits = 0; !done; ++visits) {
+        if (visits >= hd->node_count || node >= hd->node_count) {
+            report_error(err, RT_ERR_BOUNDS, 0x75000000u | node);
+            break;
+        }
+        NodeWords nd = load_node(nodes, node);
+        uint32_t nh, ph;
+        isect_node(r, nd, tmin, h.t, nh, ph);
+        if (stats) stats[0]++;
+        const uint32_t pbase = nd.w1.y;
+        while (ph && !(ANY && h.found)) {
+            uint32_t i = __ffs(ph) - 1;
+            ph &= ph - 1u;
+            InstRec ir = load_inst(prims, pbase + i);
+            if (((ir.cim >> 24) & cull_mask) == 0u) continue;
+            float o2[3], d2[3];
+            xform_point(ir.w2o, o, o2);
+            xform_vector(ir.w2o, d, d2);
+            Ray r2;
+            ray_setup(r2, o2, d2);
+            const uint8_t *blas = reinterpret_cast<const uint8_t *>(ir.accel_ref);
+            bool hit = traverse_blas_simple<ANY>(blas, r2, tmin, h, hkey, ir.id, err, stats);
+            // instances occur once in a TLAS: a best hit carrying this id
+            // was found in this instance's BLAS
+            if (h.found && h.inst == ir.id) {
+                ids.custom = ir.cim & 0xffffffu;
+                ids.sbt_off = ir.sof & 0xffffffu;
+                hit_blas = blas;
+            }
+            if (ANY && hit) break;
+        }
+        if (ANY && h.found) break;
+        uint2 g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
+        for (;;) {
+            if (g.y & 0xffu) {
+                uint32_t k = __ffs(g.y & 0xffu) - 1;
+                g.y &= ~(1u << k);
+                uint32_t s = k ^ r.oct;
+                node = g.x + __popc((g.y >> 8) & ((1u << s) - 1u));
+                if (g.y & 0xffu) {
+                    if (st.sp >= kMaxDepth) {
+                        report_error(err, RT_ERR_BOUNDS, 0x71000000u);
+                        done = true;
+                        break;
+                    }
+                    st.e[st.sp++] = g;
+                }
+                break;
+            }
+            if (st.sp == 0) { done = true; break; }
+            g = st.e[--st.sp];
+        }
+    }
+    if (h.found && hit_blas) {
+        const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(hit_blas);
+        const uint4 *bp = reinterpret_cast<const uint4 *>(hit_blas + bh->prim_offset);
+        ids.geom = ldg4(bp + (size_t)h.rec * 3u + 1).w;
+        ids.prim = ldg4(bp + (size_t)h.rec * 3u + 2).w;
+    }
+    return h.found;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent BLAS traversal (batch API hot path)
+// ---------------------------------------------------------------------------
+
+struct BatchArgs {
+    const uint8_t *accel;
+    const float4 *rays;      // 2 float4 per ray
+    float4 *hits;            // closest: 1 float4 per ray (t, prim bits, u, v)
+    rt_hit_ext *hits_ext;    // nullable
+    uint8_t *occluded;       // any-hit output
+    uint32_t n;
+    uint32_t refill;         // refill when at least this many lanes are idle
+    uint32_t *counter;
+    uint32_t *err;
+    unsigned long long *stats;
+};
+
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_blas(const BatchArgs a) {
+    __shared__ uint2 s_stack[kRing][kTraceThreads];
+    const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
+    const uint4 *nodes = reinterpret_cast<const uint4 *>(a.accel + hd->node_offset);
+    const uint4 *prims = reinterpret_cast<const uint4 *>(a.accel + hd->prim_offset);
+    const bool empty = hd->prim_count == 0;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (hd->kind != RT_ACCEL_KIND_BLAS) return;  // k_trace_tlas handles it
+
+    bool active = false, exhausted = false;
+    uint32_t ray_idx = 0;
+    Ray r;
+    float tmin = 0.f;
+    Hit h;
+    h.t = 0.f; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.inst = 0; h.found = false;
+    uint32_t node = 0;
+    bool pending = false;
+    uint2 g = make_uint2(0u, 0u);
+    int sp = 0, lo = 0;
+    uint2 spill[kMaxDepth];
+    unsigned long long n_nodes = 0, n_tris = 0;
+    // A tree walk visits each node at most once: more visits, or a node index
+    // past the end, can only come from a corrupt structure.
+    const uint32_t max_visits = hd->node_count;
+    uint32_t visits = 0;
+
+    for (;;) {
+        // ---- refill idle lanes from the global counter
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= (int)a.refill) {
+            const uint32_t cnt = __popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.counter, cnt);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + cnt >= a.n) exhausted = true;
+            if (!active) {
+                const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+                if (idx < a.n) {
+                    const float4 r0 = __ldg(a.rays + 2u * idx), r1 = __ldg(a.rays + 2u * idx + 1u);
+                    const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
+                    ray_setup(r, o, d);
+                    tmin = r0.w;
+                    h.t = r1.w; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.found = false;
+                    ray_idx = idx;
+                    active = true;
+                    node = 0;          // start at the root
+                    visits = 0;
+                    pending = !empty;  // an empty structure resolves as a miss
+                    g = make_uint2(0u, 0u);
+                    sp = 0;
+                    lo = 0;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        // ---- traversal steps until too many lanes are idle
+        for (;;) {
+            if (active) {
+                bool finish = false;
+                if (pending && (visits >= max_visits || node >= max_visits)) {
+                    report_error(a.err, RT_ERR_BOUNDS, 0x76000000u | ray_idx);
+                    pending = false;
+                    finish = true;
+                }
+                if (pending) {
+                    pending = false;
+                    ++visits;
+                    NodeWords nd = load_node(nodes, node);
+                    uint32_t nh, ph;
+                    isect_node(r, nd, tmin, h.t, nh, ph);
+                    if (STATS) n_nodes++;
+                    const uint32_t pbase = nd.w1.y;
+                    while (ph) {
+                        const uint32_t i = __ffs(ph) - 1;
+                        ph &= ph - 1u;
+                        const uint4 *rec = prims + (size_t)(pbase + i) * 3u;
+                        const uint4 q0 = ldg4(rec), q1 = ldg4(rec + 1), q2 = ldg4(rec + 2);
+                        if (STATS) n_tris++;
+                        float t, u, v;
+                        if (!isect_tri(r,
+                                       make_float4(__uint_as_float(q0.x), __uint_as_float(q0.y),
+                                                   __uint_as_float(q0.z), 0.f),
+                                       make_float4(__uint_as_float(q1.x), __uint_as_float(q1.y),
+                                                   __uint_as_float(q1.z), 0.f),
+                                       make_float4(__uint_as_float(q2.x), __uint_as_float(q2.y),
+                                                   __uint_as_float(q2.z), 0.f),
+                                       tmin, h.t, t, u, v))
+                            continue;
+                        if (ANY) {
+                            h.t = t; h.found = true;
+                            finish = true;
+                            break;
+                        }
+                        if (t < h.t || (t == h.t && q0.w < h.tri)) {
+                            h.t = t; h.u = u; h.v = v; h.rec = pbase + i; h.tri = q0.w; h.found = true;
+                        }
+                    }
+                    g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
+                }
+                // ---- next node: from the current group, else pop
+                while (!finish) {
+                    if (g.y & 0xffu) {
+                        const uint32_t k = __ffs(g.y & 0xffu) - 1;
+                        g.y &= ~(1u << k);
+                        const uint32_t s = k ^ r.oct;
+                        node = g.x + __popc((g.y >> 8) & ((1u << s) - 1u));
+                        pending = true;
+                        if (g.y & 0xffu) {
+                            if (sp >= kMaxDepth) {
+                                report_error(a.err, RT_ERR_BOUNDS, 0x72000000u | ray_idx);
+                                finish = true;
+                                break;
+                            }
+                            if (sp - lo == kRing) {
+                                spill[lo] = s_stack[lo & (kRing - 1)][tid];
+                                ++lo;
+                            }
+                            s_stack[sp & (kRing - 1)][tid] = g;
+                            ++sp;
+                        }
+                        break;
+                    }
+                    if (sp == 0) { finish = true; break; }
+                    --sp;
+                    if (sp >= lo) {
+                        g = s_stack[sp & (kRing - 1)][tid];
+                    } else {
+                        g = spill[sp];
+                        lo = sp;
+                    }
+                }
+                if (finish) {
+                    // ---- write the result
+                    if (ANY) {
+                        if (a.occluded) a.occluded[ray_idx] = h.found ? 1u : 0u;
+                    } else {
+                        float4 out;
+                        if (h.found) out = make_float4(h.t, __uint_as_float(h.tri), h.u, h.v);
+                        else out = make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
+                        if (a.hits) a.hits[ray_idx] = out;
+                        if (a.hits_ext) {
+                            rt_hit_ext x;
+                            x.t = out.x; x.u = out.z; x.v = out.w;
+                            x.instance_id = h.found ? 0u : kNone;
+                            x.custom_index = 0;
+                            x.geometry_index = h.found ? ldg4(prims + (size_t)h.rec * 3u + 1).w : 0u;
+                            x.primitive_id = h.found ? ldg4(prims + (size_t)h.rec * 3u + 2).w : kNone;
+                            x.sbt_record = x.geometry_index;
+                            a.hits_ext[ray_idx] = x;
+                        }
+                    }
+                    active = false;
+                    pending = false;
+                }
+            }
+            const uint32_t act = __ballot_sync(0xffffffffu, active);
+            if (act == 0u) break;
+            if (!exhausted && (uint32_t)__popc(~act) >= a.refill) break;
+        }
+    }
+    if (STATS) {
+        for (int o = 16; o > 0; o >>= 1) {
+            n_nodes += __shfl_xor_sync(0xffffffffu, n_nodes, o);
+            n_tris += __shfl_xor_sync(0xffffffffu, n_tris, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, n_nodes);
+            atomicAdd(a.stats + 1, n_tris);
+        }
+    }
+}
+
+// Two-level structures (instances): one ray per thread, grid-stride, through
+// the per-thread path.  Launched beside k_trace_blas; each kernel returns at
+// once when the structure is not its kind, so the host never reads it.
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_tlas(const BatchArgs a) {
+    const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
+    if (hd->kind != RT_ACCEL_KIND_TLAS) return;
+    const int tid = threadIdx.x;
+    // Two-level structures: one ray per thread, grid-stride, through the
+    // per-thread path (instance transforms need a second ray setup).
+    unsigned long long st2[2] = {0ull, 0ull};
+    for (uint32_t i = blockIdx.x * blockDim.x + tid; i < a.n; i += gridDim.x * blockDim.x) {
+        const float4 r0 = __ldg(a.rays + 2u * i), r1 = __ldg(a.rays + 2u * i + 1u);
+        const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
+        Hit th;
+        HitIds ids;
+        bool hit = trace_ray<ANY>(a.accel, o, d, r0.w, r1.w, 0xffu, th, ids, a.err, STATS ? st2 : nullptr);
+        if (ANY) {
+            if (a.occluded) a.occluded[i] = hit ? 1u : 0u;
+        } else {
+            float4 out = th.found ? make_float4(th.t, __uint_as_float(th.tri), th.u, th.v)
+                                  : make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
+            if (a.hits) a.hits[i] = out;
+            if (a.hits_ext) {
+                rt_hit_ext x;
+                x.t = out.x; x.u = out.z; x.v = out.w;
+                x.instance_id = th.found ? th.inst : kNone;
+                x.custom_index = th.found ? ids.custom : 0u;
+                x.geometry_index = th.found ? ids.geom : 0u;
+                x.primitive_id = th.found ? ids.prim : kNone;
+                x.sbt_record = th.found ? ids.sbt_off + ids.geom : 0u;
+                a.hits_ext[i] = x;
+            }
+        }
+    }
+    if (STATS) {
+        atomicAdd(a.stats, st2[0]);
+        atomicAdd(a.stats + 1, st2[1]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sample pipeline: raygen + trace + closest-hit/miss + imageStore
+// ---------------------------------------------------------------------------
+
+struct PipelineArgs {
+    const uint8_t *accel;
+    float cam[3];
+    float ay, ax;   // aspect_y, aspect_x of the raygen (host-computed)
+    uint32_t width, height;
+    uint32_t chit, ray_flags, cull_mask, sbt_record_offset, sbt_record_stride;
+    float tmin, tmax;
+    float miss[3];
+    const float *sbt;
+    uint32_t sbt_count, sbt_stride;
+    float4 *out;
+    rt_ray *rays_out;  // when set: write the primary rays instead of tracing
+    uint32_t *err;
+};
+
+// The sample's raygen (main.cpp:1036-1045), one IEEE operation at a time.
+__device__ __forceinline__ void raygen(const PipelineArgs &a, uint32_t x, uint32_t y, float dir[3]) {
+    const float sx = (float)x + 0.5f, sy = (float)y + 0.5f;
+    const float ndx = (sx / (float)a.width) * 2.0f - 1.0f;
+    const float ndy = (sy / (float)a.height) * 2.0f - 1.0f;
+    const float p = ndx * a.ax, q = ndy * a.ay;
+    dir[0] = (p * 1.0f + q * 0.0f) + 0.0f;
+    dir[1] = (p * 0.0f + q * -1.0f) + 0.0f;
+    dir[2] = (p * 0.0f + q * 0.0f) + -1.0f;
+}
+
+__global__ void __launch_bounds__(128) k_pipeline(const PipelineArgs a) {
+    const uint32_t x = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t y = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (x >= a.width || y >= a.height) return;
+    float dir[3];
+    raygen(a, x, y, dir);
+    const size_t pix = (size_t)y * a.width + x;
+    if (a.rays_out) {
+        rt_ray rr;
+        rr.org[0] = a.cam[0]; rr.org[1] = a.cam[1]; rr.org[2] = a.cam[2];
+        rr.dir[0] = dir[0]; rr.dir[1] = dir[1]; rr.dir[2] = dir[2];
+        rr.tmin = a.tmin;
+        rr.tmax = a.tmax;
+        a.rays_out[pix] = rr;
+        return;
+    }
+    Hit h;
+    HitIds ids;
+    float c[3];
+    if (a.ray_flags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT)
+        trace_ray<true>(a.accel, a.cam, dir, a.tmin, a.tmax, a.cull_mask & 0xffu, h, ids, a.err, nullptr);
+    else
+        trace_ray<false>(a.accel, a.cam, dir, a.tmin, a.tmax, a.cull_mask & 0xffu, h, ids, a.err, nullptr);
+    if (!h.found) {
+        c[0] = a.miss[0]; c[1] = a.miss[1]; c[2] = a.miss[2];
+    } else if (a.ray_flags & RT_RAY_FLAG_SKIP_CLOSEST_HIT) {
+        c[0] = c[1] = c[2] = 0.0f;
+    } else {
+        const uint32_t rec = ids.sbt_off + ids.geom * a.sbt_record_stride + a.sbt_record_offset;
+        const bool bary = a.chit == RT_CHIT_BARYCENTRIC ||
+                          (a.chit == RT_CHIT_SAMPLE && ids.prim == 1u && h.inst == 1u && ids.custom == 100u &&
+                           ids.geom == 1u);
+        if (bary) {
+            c[0] = (1.0f - h.u) - h.v; c[1] = h.u; c[2] = h.v;
+        } else if (rec < a.sbt_count) {
+            c[0] = a.sbt[(size_t)rec * a.sbt_stride + 0];
+            c[1] = a.sbt[(size_t)rec * a.sbt_stride + 1];
+            c[2] = a.sbt[(size_t)rec * a.sbt_stride + 2];
+        } else {
+            c[0] = c[1] = c[2] = 0.0f;
+            report_error(a.err, RT_ERR_BOUNDS, 0x73000000u | rec);
+        }
+    }
+    a.out[pix] = make_float4(c[0], c[1], c[2], 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *rays, rt_hit *hits,
+                 rt_hit_ext *hits_ext, uint8_t *occ, uint32_t n, bool any, unsigned long long *stats) {
+    if (n == 0) return RT_OK;
+    BatchArgs a;
+    a.accel = reinterpret_cast<const uint8_t *>(accel);
+    a.rays = reinterpret_cast<const float4 *>(rays);
+    a.hits = reinterpret_cast<float4 *>(hits);
+    a.hits_ext = hits_ext;
+    a.occluded = occ;
+    a.n = n;
+    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 8u;
+    if (a.refill > 32u) a.refill = 32u;
+    a.err = ctx->d_err;
+    a.stats = stats;
+    a.counter = acquire_counter(ctx, st);
+    if (!a.counter) return set_error(ctx, RT_ERR_CUDA, "work counter reset failed");
+    uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
+    uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
+    uint32_t need = (n + kTraceThreads - 1) / kTraceThreads;
+    if (blocks > need) blocks = need;
+    // Both kernels are launched; the one that does not match the structure's
+    // kind returns immediately.
+    const uint32_t tl_blocks = (uint32_t)ctx->sm_count * 4u < need ? (uint32_t)ctx->sm_count * 4u : need;
+    if (stats) {
+        if (any) {
+            k_trace_blas<true, true><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_tlas<true, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+        } else {
+            k_trace_blas<false, true><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_tlas<false, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+        }
+    } else {
+        if (any) {
+            k_trace_blas<true, false><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_tlas<true, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+        } else {
+            k_trace_blas<false, false><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_tlas<false, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+        }
+    }
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *ay, float *ax) {
+    // aspect_y = tan(radians(yFov) * 0.5) (main.cpp:1039): radians and the
+    // halving in float as GLSL evaluates them, tan in double rounded once.
+    const float half = (cam->y_fov_degree * (float)(3.14159265358979323846 / 180.0)) * 0.5f;
+    *ay = (float)std::tan((double)half);
+    *ax = (*ay * (float)w) / (float)h;
+}
+
+}  // namespace
+}  // namespace rtc
+
+using namespace rtc;
+
+extern "C" rt_status rt_trace_closest(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                      rt_hit *hits, rt_hit_ext *hits_ext, uint32_t n) {
+    if (!ctx || !accel || (n && (!rays || !hits))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_closest: null argument");
+    return launch_batch(ctx, static_cast<cudaStream_t>(stream), accel, rays, hits, hits_ext, nullptr, n, false,
+                        nullptr);
+}
+
+extern "C" rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                  uint8_t *occluded, uint32_t n) {
+    if (!ctx || !accel || (n && (!rays || !occluded))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_any: null argument");
+    return launch_batch(ctx, static_cast<cudaStream_t>(stream), accel, rays, nullptr, nullptr, occluded, n, true,
+                        nullptr);
+}
+
+extern "C" rt_status rt_trace_stats(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                    uint32_t n, int any_hit, unsigned long long *counters) {
+    if (!ctx || !accel || !counters || (n && !rays)) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_stats: null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(counters, 0, 16, st));
+    // No hit output: the counters are the result.
+    return launch_batch(ctx, st, accel, rays, nullptr, nullptr, nullptr, n, any_hit != 0, counters);
+}
+
+extern "C" rt_status rt_trace_rays(rt_context *ctx, rt_stream stream, const rt_pipeline *p, const rt_sbt *sbt,
+                                   uint64_t accel, const rt_camera *camera, float *out, uint32_t width,
+                                   uint32_t height, uint32_t depth) {
+    if (!ctx || !p || !accel || !camera || !out) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_rays: null argument");
+    if (depth != 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_trace_rays: depth must be 1 (2D storage image)");
+    if (width == 0 || height == 0) return RT_OK;
+    if (p->chit > RT_CHIT_SBT_COLOR) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_rays: unknown closest-hit program");
+    if (p->max_recursion > 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_trace_rays: recursion depth > 1");
+    if (p->sbt_record_stride == 0u && p->chit != RT_CHIT_BARYCENTRIC)
+        ; /* stride 0 is legal in Vulkan: every geometry uses the same record */
+    PipelineArgs a;
+    a.accel = reinterpret_cast<const uint8_t *>(accel);
+    a.cam[0] = camera->position[0]; a.cam[1] = camera->position[1]; a.cam[2] = camera->position[2];
+    camera_aspects(camera, width, height, &a.ay, &a.ax);
+    a.width = width;
+    a.height = height;
+    a.chit = p->chit;
+    a.ray_flags = p->ray_flags;
+    a.cull_mask = p->cull_mask;
+    a.sbt_record_offset = p->sbt_record_offset;
+    a.sbt_record_stride = p->sbt_record_stride;
+    a.tmin = p->tmin;
+    a.tmax = p->tmax;
+    a.miss[0] = p->miss_color[0]; a.miss[1] = p->miss_color[1]; a.miss[2] = p->miss_color[2];
+    a.sbt = sbt ? sbt->hit_colors : nullptr;
+    a.sbt_count = sbt && sbt->hit_colors ? sbt->hit_record_count : 0u;
+    a.sbt_stride = sbt ? (sbt->hit_record_stride < 3u ? 3u : sbt->hit_record_stride) : 3u;
+    a.out = reinterpret_cast<float4 *>(out);
+    a.rays_out = nullptr;
+    a.err = ctx->d_err;
+    dim3 grid((width + 15u) / 16u, (height + 7u) / 8u);
+    k_pipeline<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+extern "C" rt_status rt_generate_primary_rays(rt_context *ctx, rt_stream stream, const rt_camera *camera,
+                                              uint32_t width, uint32_t height, float tmin, float tmax,
+                                              rt_ray *rays) {
+    if (!ctx || !camera || !rays) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_generate_primary_rays: null argument");
+    if (width == 0 || height == 0) return RT_OK;
+    PipelineArgs a{};
+    a.cam[0] = camera->position[0]; a.cam[1] = camera->position[1]; a.cam[2] = camera->position[2];
+    camera_aspects(camera, width, height, &a.ay, &a.ax);
+    a.width = width;
+    a.height = height;
+    a.tmin = tmin;
+    a.tmax = tmax;
+    a.rays_out = rays;
+    a.err = ctx->d_err;
+    dim3 grid((width + 15u) / 16u, (height + 7u) / 8u);
+    k_pipeline<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}

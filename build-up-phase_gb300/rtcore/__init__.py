@@ -1,0 +1,327 @@
+"""Python binding of librtcore (the GB300 software ray-tracing core).
+
+A thin ctypes mirror of include/rtcore.h: the same entry points, argument
+meaning and status codes as the C ABI.  Device buffers are passed as raw
+pointers; torch tensors are accepted for convenience (torch is only the
+allocator and stream provider here).  There is no fallback: if the CUDA
+library is missing or fails to load, every call raises.
+
+The entry points mirror the Vulkan calls of the reference sample
+(vulkan-raytraced-triangle/main.cpp): rt_get_*_build_sizes ->
+vkGetAccelerationStructureBuildSizesKHR (:757, :893), rt_build_* ->
+vkCmdBuildAccelerationStructuresKHR (:808, :932), rt_trace_rays ->
+vkCmdTraceRaysKHR (:1349).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_DIR / "lib" / "librtcore.so"
+
+# ---------------------------------------------------------------------------
+# status codes and flags (rtcore.h)
+# ---------------------------------------------------------------------------
+RT_OK = 0
+RT_ERR_INVALID_ARG = -1
+RT_ERR_OOM = -2
+RT_ERR_CUDA = -3
+RT_ERR_TIMEOUT = -4
+RT_ERR_BOUNDS = -5
+RT_ERR_UNSUPPORTED = -6
+RT_ERR_NO_DEVICE = -7
+STATUS_NAMES = {0: "RT_OK", -1: "RT_ERR_INVALID_ARG", -2: "RT_ERR_OOM", -3: "RT_ERR_CUDA",
+                -4: "RT_ERR_TIMEOUT", -5: "RT_ERR_BOUNDS", -6: "RT_ERR_UNSUPPORTED",
+                -7: "RT_ERR_NO_DEVICE"}
+
+RT_INDEX_NONE = 0
+RT_INDEX_UINT32 = 1
+RT_GEOMETRY_OPAQUE = 1
+RT_BUILD_PREFER_FAST_TRACE = 1 << 0
+RT_BUILD_MORTON30 = 1 << 8
+RT_BUILD_MORTON63 = 1 << 9
+RT_RAY_FLAG_OPAQUE = 1 << 0
+RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT = 1 << 2
+RT_RAY_FLAG_SKIP_CLOSEST_HIT = 1 << 3
+RT_CHIT_SAMPLE = 0
+RT_CHIT_BARYCENTRIC = 1
+RT_CHIT_SBT_COLOR = 2
+RT_NO_HIT = 0xFFFFFFFF
+RT_GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE = 1
+
+
+class RtError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str = ""):
+        self.code = code
+        super().__init__(f"{where}: {STATUS_NAMES.get(code, code)}" + (f" ({msg})" if msg else ""))
+
+
+# ---------------------------------------------------------------------------
+# structs
+# ---------------------------------------------------------------------------
+class Transform3x4(C.Structure):
+    _fields_ = [("m", (C.c_float * 4) * 3)]
+
+
+class GeometryTriangles(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("vertex_stride", C.c_uint64), ("max_vertex", C.c_uint32),
+                ("index_type", C.c_uint32), ("indices", C.c_void_p), ("tri_count", C.c_uint32),
+                ("flags", C.c_uint32), ("transform", C.c_void_p)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("transform", Transform3x4), ("custom_index_and_mask", C.c_uint32),
+                ("sbt_offset_and_flags", C.c_uint32), ("accel_ref", C.c_uint64)]
+
+
+class BuildSizes(C.Structure):
+    _fields_ = [("accel_bytes", C.c_uint64), ("scratch_bytes", C.c_uint64)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("y_fov_degree", C.c_float)]
+
+
+class Pipeline(C.Structure):
+    _fields_ = [("chit", C.c_uint32), ("ray_flags", C.c_uint32), ("cull_mask", C.c_uint32),
+                ("sbt_record_offset", C.c_uint32), ("sbt_record_stride", C.c_uint32),
+                ("miss_index", C.c_uint32), ("tmin", C.c_float), ("tmax", C.c_float),
+                ("miss_color", C.c_float * 3), ("max_recursion", C.c_uint32)]
+
+
+class Sbt(C.Structure):
+    _fields_ = [("hit_colors", C.c_void_p), ("hit_record_count", C.c_uint32),
+                ("hit_record_stride", C.c_uint32)]
+
+
+class TraceTuning(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("batch_rays", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+assert C.sizeof(GeometryTriangles) == 48
+assert C.sizeof(Instance) == 64
+assert C.sizeof(Camera) == 16
+
+# Every symbol include/rtcore.h declares, with (restype, argtypes).
+_vp, _u32, _u64, _i32, _f = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+PROTOTYPES = {
+    "rt_context_create": (_i32, [_i32, C.POINTER(_vp)]),
+    "rt_context_destroy": (_i32, [_vp]),
+    "rt_last_error_string": (C.c_char_p, [_vp]),
+    "rt_sync": (_i32, [_vp, _vp]),
+    "rt_abi_version": (_u32, []),
+    "rt_get_blas_build_sizes": (_i32, [_vp, C.POINTER(_u32), _u32, _u32, C.POINTER(BuildSizes)]),
+    "rt_get_tlas_build_sizes": (_i32, [_vp, _u32, _u32, C.POINTER(BuildSizes)]),
+    "rt_build_blas": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _u32, _vp, _u64, _vp, _u64]),
+    "rt_build_tlas": (_i32, [_vp, _vp, _vp, _u32, _u32, _vp, _u64, _vp, _u64]),
+    "rt_accel_address": (_u64, [_vp]),
+    "rt_accel_info": (_i32, [_vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "rt_trace_rays": (_i32, [_vp, _vp, C.POINTER(Pipeline), C.POINTER(Sbt), _u64, C.POINTER(Camera), _vp,
+                             _u32, _u32, _u32]),
+    "rt_trace_closest": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _u32]),
+    "rt_trace_any": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32]),
+    "rt_generate_primary_rays": (_i32, [_vp, _vp, C.POINTER(Camera), _u32, _u32, _f, _f, _vp]),
+    "rt_trace_stats": (_i32, [_vp, _vp, _u64, _vp, _u32, _i32, _vp]),
+    "rt_set_trace_tuning": (_i32, [_vp, C.POINTER(TraceTuning)]),
+    "rt_get_trace_tuning": (_i32, [_vp, C.POINTER(TraceTuning)]),
+    "rt_write_ppm": (_i32, [_vp, _u32, _u32, C.c_char_p]),
+    "rt_write_pfm": (_i32, [_vp, _u32, _u32, C.c_char_p]),
+    # debug / utility entry points declared in include/rtcore_debug.h
+    "rt_get_sort_scratch_bytes": (_i32, [_u32, _u32, C.POINTER(_u64)]),
+    "rt_sort_pairs": (_i32, [_vp, _vp, _vp, _vp, _u32, _u32, _vp, _u64]),
+    "rt_debug_blas_scratch_layout": (_i32, [_u32, _u32, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    # seeded scenes declared in include/rtcore_scene.h (host code)
+    "rt_scene_soup": (_i32, [_u64, _u32, _vp, _vp]),
+    "rt_scene_box_counts": (_i32, [_u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "rt_scene_box": (_i32, [_u64, _u32, _u32, _vp, _vp, _vp, _vp]),
+    "rt_scene_incoherent_rays": (_i32, [_u64, _u32, _vp, _vp, _f, _vp]),
+}
+
+_lib = None
+
+
+def lib_path() -> Path:
+    return LIB_PATH
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads librtcore.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RtError(RT_ERR_NO_DEVICE, "load", f"{p} is missing; build it with build-up-phase_gb300/build.py")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(x) -> int | None:
+    """Device pointer of a torch tensor, an int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Context:
+    """rt_context: owner of the device-side bookkeeping of the core."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.rt_context_create(device, C.byref(h))
+        if rc != RT_OK:
+            raise RtError(rc, "rt_context_create")
+        self.h = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.rt_context_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc: int, where: str) -> None:
+        if rc != RT_OK:
+            msg = self.lib.rt_last_error_string(self.h)
+            raise RtError(rc, where, msg.decode() if msg else "")
+
+    # ---- sizes / builds
+    def blas_sizes(self, tri_counts, flags: int = 0) -> BuildSizes:
+        arr = (C.c_uint32 * max(1, len(tri_counts)))(*tri_counts)
+        out = BuildSizes()
+        self.check(self.lib.rt_get_blas_build_sizes(self.h, arr, len(tri_counts), flags, C.byref(out)),
+                   "rt_get_blas_build_sizes")
+        return out
+
+    def tlas_sizes(self, n: int, flags: int = 0) -> BuildSizes:
+        out = BuildSizes()
+        self.check(self.lib.rt_get_tlas_build_sizes(self.h, n, flags, C.byref(out)), "rt_get_tlas_build_sizes")
+        return out
+
+    def build_blas(self, geoms, flags, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
+        arr = (GeometryTriangles * max(1, len(geoms)))(*geoms)
+        self.check(self.lib.rt_build_blas(self.h, _stream_ptr(stream), arr, len(geoms), flags, _ptr(accel),
+                                          accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_blas")
+
+    def build_tlas(self, instances, n, flags, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
+        self.check(self.lib.rt_build_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, flags, _ptr(accel),
+                                          accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_tlas")
+
+    def accel_info(self, accel, stream=None):
+        nc, pc, d = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self.check(self.lib.rt_accel_info(self.h, _stream_ptr(stream), _ptr(accel), C.byref(nc), C.byref(pc),
+                                          C.byref(d)), "rt_accel_info")
+        return nc.value, pc.value, d.value
+
+    def address(self, accel) -> int:
+        return int(self.lib.rt_accel_address(_ptr(accel)))
+
+    # ---- tracing
+    def trace_closest(self, accel_addr: int, rays, hits, n: int, hits_ext=None, stream=None) -> None:
+        self.check(self.lib.rt_trace_closest(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(hits),
+                                             _ptr(hits_ext), n), "rt_trace_closest")
+
+    def trace_any(self, accel_addr: int, rays, occluded, n: int, stream=None) -> None:
+        self.check(self.lib.rt_trace_any(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(occluded), n),
+                   "rt_trace_any")
+
+    def trace_stats(self, accel_addr: int, rays, n: int, any_hit: bool, counters, stream=None) -> None:
+        self.check(self.lib.rt_trace_stats(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), n,
+                                           1 if any_hit else 0, _ptr(counters)), "rt_trace_stats")
+
+    def trace_rays(self, pipeline: Pipeline, sbt: Sbt | None, accel_addr: int, camera: Camera, out, width: int,
+                   height: int, depth: int = 1, stream=None) -> None:
+        self.check(self.lib.rt_trace_rays(self.h, _stream_ptr(stream), C.byref(pipeline),
+                                          C.byref(sbt) if sbt is not None else None, accel_addr, C.byref(camera),
+                                          _ptr(out), width, height, depth), "rt_trace_rays")
+
+    def generate_primary_rays(self, camera: Camera, width: int, height: int, tmin: float, tmax: float, rays,
+                              stream=None) -> None:
+        self.check(self.lib.rt_generate_primary_rays(self.h, _stream_ptr(stream), C.byref(camera), width, height,
+                                                     tmin, tmax, _ptr(rays)), "rt_generate_primary_rays")
+
+    def sync(self, stream=None) -> None:
+        self.check(self.lib.rt_sync(self.h, _stream_ptr(stream)), "rt_sync")
+
+    def set_tuning(self, blocks_per_sm: int, batch_rays: int) -> None:
+        t = TraceTuning(128, blocks_per_sm, batch_rays, 0)
+        self.check(self.lib.rt_set_trace_tuning(self.h, C.byref(t)), "rt_set_trace_tuning")
+
+    def get_tuning(self) -> TraceTuning:
+        t = TraceTuning()
+        self.check(self.lib.rt_get_trace_tuning(self.h, C.byref(t)), "rt_get_trace_tuning")
+        return t
+
+    # ---- utilities
+    def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:
+        self.check(self.lib.rt_sort_pairs(self.h, _stream_ptr(stream), _ptr(keys), _ptr(vals), n, key_bits,
+                                          _ptr(scratch), scratch_bytes), "rt_sort_pairs")
+
+
+def sort_scratch_bytes(n: int, key_bits: int) -> int:
+    out = C.c_uint64()
+    rc = load().rt_get_sort_scratch_bytes(n, key_bits, C.byref(out))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_get_sort_scratch_bytes")
+    return out.value
+
+
+def blas_scratch_layout(n_tris: int, flags: int = 0):
+    k, i, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    load().rt_debug_blas_scratch_layout(n_tris, flags, C.byref(k), C.byref(i), C.byref(b))
+    return k.value, i.value, b.value
+
+
+def pack_custom_mask(custom_index: int, mask: int) -> int:
+    return (custom_index & 0xFFFFFF) | ((mask & 0xFF) << 24)
+
+
+def pack_sbt_flags(sbt_offset: int, flags: int) -> int:
+    return (sbt_offset & 0xFFFFFF) | ((flags & 0xFF) << 24)
+
+
+def sample_pipeline(chit: int = RT_CHIT_SAMPLE) -> Pipeline:
+    """The constant arguments of the sample's raygen traceRayEXT call
+    (main.cpp:1047-1052) and its miss colour (main.cpp:1065)."""
+    p = Pipeline()
+    p.chit = chit
+    p.ray_flags = RT_RAY_FLAG_OPAQUE
+    p.cull_mask = 0xFF
+    p.sbt_record_offset = 0
+    p.sbt_record_stride = 1
+    p.miss_index = 0
+    p.tmin = 0.0
+    p.tmax = 100.0
+    p.miss_color[:] = [0.0, 0.0, 0.2]
+    p.max_recursion = 1
+    return p

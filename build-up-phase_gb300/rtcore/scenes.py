@@ -1,0 +1,90 @@
+"""Seeded synthetic workloads as numpy arrays (host memory).
+
+The generators themselves are host C++ in librtcore (include/rtcore_scene.h)
+so that the C++ drop-in sample and the Python tests and benchmark produce the
+same bits; this module only allocates the arrays and calls them.
+
+Seeds follow one convention: 0x5EED0000 + workload number, where 1 is the
+single-triangle sample, 2 the triangle soup, 3 the box scene, 4 the batched
+form and 5 the learned form.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import RT_OK, RtError, load
+
+SEED_BASE = 0x5EED0000
+
+# rt_ray: org xyz, tmin, dir xyz, tmax (32 bytes)
+RAY_DTYPE = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+# rt_hit: t, prim, u, v (16 bytes)
+HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+# rt_hit_ext (32 bytes)
+HIT_EXT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("instance_id", "<u4"),
+                          ("custom_index", "<u4"), ("geometry_index", "<u4"), ("primitive_id", "<u4"),
+                          ("sbt_record", "<u4")])
+MATERIAL_DTYPE = np.dtype([("albedo", "<f4", 3), ("emission", "<f4", 3)])
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def soup(seed: int, n_tris: int):
+    """(vertices float32 [3n, 3], indices uint32 [n, 3]) of the triangle soup."""
+    v = np.empty((3 * n_tris, 3), np.float32)
+    i = np.empty((n_tris, 3), np.uint32)
+    rc = load().rt_scene_soup(seed, n_tris, _ptr(v), _ptr(i))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_scene_soup")
+    return v, i
+
+
+def box(seed: int, n_spheres: int, freq: int):
+    """(vertices, indices, tri_material, materials) of the box scene."""
+    lib = load()
+    nv, nt, nm = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    rc = lib.rt_scene_box_counts(n_spheres, freq, C.byref(nv), C.byref(nt), C.byref(nm))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_scene_box_counts")
+    v = np.empty((nv.value, 3), np.float32)
+    i = np.empty((nt.value, 3), np.uint32)
+    tm = np.empty(nt.value, np.uint32)
+    m = np.empty(nm.value, MATERIAL_DTYPE)
+    rc = lib.rt_scene_box(seed, n_spheres, freq, _ptr(v), _ptr(i), _ptr(tm), _ptr(m))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_scene_box")
+    return v, i, tm, m
+
+
+def incoherent_rays(seed: int, n: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), tmax: float = 1e30):
+    rays = np.empty(n, RAY_DTYPE)
+    lo_a = np.asarray(lo, np.float32)
+    hi_a = np.asarray(hi, np.float32)
+    rc = load().rt_scene_incoherent_rays(seed, n, _ptr(lo_a), _ptr(hi_a), tmax, _ptr(rays))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_scene_incoherent_rays")
+    return rays
+
+
+# The reference sample's scene (vulkan-raytraced-triangle/main.cpp).
+REF8_VERTICES = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], np.float32)       # :676-681
+REF8_INDICES = np.array([[0, 1, 3], [1, 2, 3]], np.uint32)                                 # :682
+REF8_GEOM_TRANSFORMS = np.array([[[1, 0, 0, -2], [0, 1, 0, 0], [0, 0, 1, 0]],               # :684-695
+                                 [[1, 0, 0, 2], [0, 1, 0, 0], [0, 0, 1, 0]]], np.float32)
+REF8_INSTANCE_TRANSFORMS = np.array([[[1, 0, 0, 0], [0, 1, 0, 2], [0, 0, 1, 0]],           # :835-846
+                                     [[1, 0, 0, 0], [0, 1, 0, -2], [0, 0, 1, 0]]], np.float32)
+REF8_CUSTOM_INDEX = 100                                                                    # :850
+REF8_SBT_OFFSETS = (0, 2)                                                                  # :851, :857
+REF8_SBT_COLORS = np.array([[0.6, 0.1, 0.2], [0.1, 0.8, 0.4], [0.9, 0.7, 0.1], [0.3, 0.6, 0.9]],
+                           np.float32)                                                     # :1310-1317
+REF8_CAMERA = ((0.0, 0.0, 10.0), 60.0)                                                     # :1015
+REF8_SIZE = (1200, 800)                                                                    # :13-14
+
+TRI1_VERTICES = np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], np.float32)
+TRI1_INDICES = np.array([[0, 1, 2]], np.uint32)
+TRI1_CAMERA = ((0.0, 0.0, 2.5), 60.0)
+TRI1_SIZE = (800, 600)

@@ -1,0 +1,176 @@
+"""GPU parity of the acceleration-structure build (through the C ABI):
+Morton keys, sort order, radix tree and the final BVH8 bytes are bit-exact
+against the CPU oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import GpuBlas, GpuTlas, compare_accels, dev, header, host, ref8_instances, ref8_items, ptr_of
+
+pytestmark = pytest.mark.gpu
+
+M30 = 1 << 8
+
+
+def soup(n, seed=21):
+    import rtcore.scenes as S
+    v, i = S.soup(seed, n)
+    return [(v, i, None)]
+
+
+@pytest.mark.parametrize("n,flags", [(0, 0), (1, 0), (2, 0), (3, 0), (4, 0), (9, 0), (100, 0), (4097, 0),
+                                     (20000, 0), (250000, 0), (20000, M30), (250000, M30)])
+def test_blas_bit_exact(ctx, orc, n, flags):
+    items = soup(n)
+    g = GpuBlas(ctx, items, flags)
+    o, rc = orc.build_blas(items, flags)
+    assert rc == 0
+    compare_accels(g.bytes(), o, 48)
+
+
+def test_blas_stages_bit_exact(ctx, orc):
+    import rtcore
+    n = 50000
+    items = soup(n, seed=5)
+    g = GpuBlas(ctx, items)
+    o, rc, (ks, ids, bn) = orc.build_blas(items, 0, debug=True)
+    koff, ioff, boff = rtcore.blas_scratch_layout(n)
+    s = host(g.scratch)
+    np.testing.assert_array_equal(s[koff:koff + 8 * n].view(np.uint64), ks)
+    np.testing.assert_array_equal(s[ioff:ioff + 4 * n].view(np.uint32), ids)
+    np.testing.assert_array_equal(s[boff:boff + 16 * (n - 1)].view(np.uint32).reshape(-1, 4), bn)
+
+
+def test_blas_duplicates_degenerates_and_bad_indices(ctx, orc):
+    # 300 identical triangles (equal Morton keys), 50 zero-area, 1 NaN vertex
+    base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    v = np.concatenate([np.tile(base, (300, 1)), np.tile(np.array([[0.5, 0.5, 0.5]] * 3, np.float32), (50, 1)),
+                        np.array([[np.nan, 0, 0], [1, 1, 1], [0, 1, 1]], np.float32)])
+    items = [(v, None, None)]
+    g = GpuBlas(ctx, items)
+    o, rc = orc.build_blas(items)
+    compare_accels(g.bytes(), o, 48)
+    # an index beyond max_vertex: the triangle is inactive, the build and
+    # rt_sync report RT_ERR_BOUNDS, nothing is read out of range
+    import rtcore
+    bad = [(base, np.array([[0, 1, 2], [0, 1, 9]], np.uint32), None)]
+    with pytest.raises(rtcore.RtError) as e:
+        GpuBlas(ctx, bad)
+    assert e.value.code == rtcore.RT_ERR_BOUNDS
+    o2, rc2 = orc.build_blas(bad)
+    assert rc2 == rtcore.RT_ERR_BOUNDS
+
+
+def test_blas_box_scene_bit_exact(ctx, orc):
+    import rtcore.scenes as S
+    v, i, tm, m = S.box(S.SEED_BASE + 3, 6, 12)
+    items = [(v, i, None)]
+    g = GpuBlas(ctx, items)
+    o, _ = orc.build_blas(items)
+    compare_accels(g.bytes(), o, 48)
+
+
+def test_blas_geometries_with_transforms(ctx, orc):
+    items = ref8_items() + soup(500, seed=2) + [(soup(64, seed=4)[0][0], None,
+                                                 np.array([[0.5, 0.1, 0, 3], [0, 2, 0, -1], [0.2, 0, 1, 0.25]],
+                                                          np.float32))]
+    g = GpuBlas(ctx, items)
+    o, _ = orc.build_blas(items)
+    compare_accels(g.bytes(), o, 48)
+
+
+def test_tlas_bit_exact(ctx, orc):
+    g = GpuBlas(ctx, ref8_items())
+    ob, _ = orc.build_blas(ref8_items())
+    compare_accels(g.bytes(), ob, 48)
+    gt = GpuTlas(ctx, ref8_instances([g.addr, g.addr]))
+    ot, rc = orc.build_tlas(ref8_instances([ptr_of(ob), ptr_of(ob)]))
+    assert rc == 0
+    compare_accels(gt.bytes(), ot, 80, ignore_ref=True)
+
+
+def test_tlas_many_instances(ctx, orc):
+    """300 instances with rotations/scales over two BLASes."""
+    from oracle import INSTANCE_DTYPE
+    a_items, b_items = soup(200, seed=8), ref8_items()
+    ga, gb = GpuBlas(ctx, a_items), GpuBlas(ctx, b_items)
+    oa, _ = orc.build_blas(a_items)
+    ob, _ = orc.build_blas(b_items)
+    rng = np.random.default_rng(3)
+    n = 300
+    inst_g = np.zeros(n, INSTANCE_DTYPE)
+    for k in range(n):
+        ang = rng.uniform(0, 6.28)
+        s = rng.uniform(0.5, 2)
+        m = np.array([[np.cos(ang) * s, -np.sin(ang) * s, 0, rng.uniform(-5, 5)],
+                      [np.sin(ang) * s, np.cos(ang) * s, 0, rng.uniform(-5, 5)],
+                      [0, 0, s, rng.uniform(-5, 5)]], np.float32)
+        inst_g[k]["transform"] = m
+        inst_g[k]["custom_index_and_mask"] = k | (0xFF << 24)
+        inst_g[k]["sbt_offset_and_flags"] = (k % 4) | (1 << 24)
+    inst_o = inst_g.copy()
+    inst_g["accel_ref"] = [ga.addr if k % 3 else gb.addr for k in range(n)]
+    inst_o["accel_ref"] = [ptr_of(oa) if k % 3 else ptr_of(ob) for k in range(n)]
+    gt = GpuTlas(ctx, inst_g)
+    ot, _ = orc.build_tlas(inst_o)
+    compare_accels(gt.bytes(), ot, 80, ignore_ref=True)
+
+
+@pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 100003, 1 << 20])
+@pytest.mark.parametrize("dist", ["random", "equal", "few", "descending"])
+def test_sort_pairs_matches_stable_sort(ctx, orc, n, dist):
+    import rtcore
+    import torch
+    rng = np.random.default_rng(n)
+    if dist == "random":
+        keys = rng.integers(0, 1 << 63, n, dtype=np.uint64)
+    elif dist == "equal":
+        keys = np.full(n, 0x123456789, np.uint64)
+    elif dist == "few":
+        keys = rng.integers(0, 4, n, dtype=np.uint64) << np.uint64(40)
+    else:
+        keys = np.arange(n, 0, -1, dtype=np.uint64)
+    vals = np.arange(n, dtype=np.uint32)
+    for bits in (64, 30, 20):
+        mask = np.uint64((1 << bits) - 1) if bits < 64 else np.uint64(0xFFFFFFFFFFFFFFFF)
+        kd, vd = dev(keys), dev(vals)
+        nb = rtcore.sort_scratch_bytes(n, bits)
+        scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        ctx.sort_pairs(kd, vd, n, bits, scratch, nb)
+        ctx.sync()
+        order = np.argsort(keys & mask, kind="stable")
+        np.testing.assert_array_equal(host(vd).view(np.uint32), vals[order])
+        np.testing.assert_array_equal(host(kd).view(np.uint64), keys[order])
+
+
+def test_build_argument_errors(ctx):
+    import rtcore
+    import torch
+    items = soup(1000)
+    g = GpuBlas(ctx, items)
+    geo = rtcore.GeometryTriangles()
+    vd = dev(items[0][0])
+    idd = dev(items[0][1])
+    geo.vertices, geo.vertex_stride, geo.max_vertex = vd.data_ptr(), 12, 2999
+    geo.index_type, geo.indices, geo.tri_count, geo.flags = 1, idd.data_ptr(), 1000, 1
+    sz = ctx.blas_sizes([1000])
+    acc = torch.empty(sz.accel_bytes, dtype=torch.uint8, device="cuda")
+    scr = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device="cuda")
+    cases = [
+        (dict(accel_bytes=sz.accel_bytes - 256), rtcore.RT_ERR_OOM),
+        (dict(scratch_bytes=sz.scratch_bytes - 1), rtcore.RT_ERR_OOM),
+        (dict(flags=M30 | (1 << 9)), rtcore.RT_ERR_INVALID_ARG),
+        (dict(accel=acc.data_ptr() + 16), rtcore.RT_ERR_INVALID_ARG),
+    ]
+    for over, code in cases:
+        kw = dict(accel=acc, accel_bytes=sz.accel_bytes, scratch=scr, scratch_bytes=sz.scratch_bytes, flags=0)
+        kw.update(over)
+        with pytest.raises(rtcore.RtError) as e:
+            ctx.build_blas([geo], kw["flags"], kw["accel"], kw["accel_bytes"], kw["scratch"], kw["scratch_bytes"])
+        assert e.value.code == code
+    ctx.sync()
+    # the earlier good build is intact
+    assert header(g.bytes())["status"] == 0
+    nodes, prims, depth = ctx.accel_info(g.accel)
+    assert prims == 1000 and 1 <= nodes <= 999 and depth >= 2
