@@ -819,7 +819,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
         k_morton<<<g, 256, 0, st>>>(boxes, n, cb, bpa, keys0, ids0, hist, passes);
         RT_CUDA_CTX(ctx, cudaGetLastError());
     }
-    int sst = sort_pairs(ctx, st, keys0, ids0, keys1, ids1, n, passes, sort_s, true, ctx->d_err);
+    int sst = sort_pairs(ctx, st, keys0, ids0, keys1, ids1, n, 8 * passes, sort_s, true, ctx->d_err);
     if (sst) return set_error(ctx, sst, "radix sort launch failed");
 
     uint4 *bin = reinterpret_cast<uint4 *>(S + L.bin);

@@ -45,7 +45,7 @@ uint32_t *acquire_counter(rt_context *ctx, cudaStream_t stream);
 // Sort (rt_sort.cu)
 uint64_t sort_scratch_bytes(uint32_t n, int passes);
 int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
-               uint32_t *vals1, uint32_t n, int passes, void *scratch, bool hist_done, uint32_t *err);
+               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err);
 uint32_t *sort_hist_ptr(void *scratch);
 
 }  // namespace rtc

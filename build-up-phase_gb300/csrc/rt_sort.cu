@@ -36,14 +36,21 @@ constexpr int kSpinLimit = 1 << 22;
 constexpr size_t kSortSmemBytes =
     (size_t)kSortTile * 8u + (size_t)kSortTile * 4u + (size_t)kSortWarps * kRadix * 4u;
 
-__global__ void __launch_bounds__(256) k_sort_hist(const uint64_t *__restrict__ keys, uint32_t n, int passes,
+// Digit mask of pass p when sorting on the low key_bits bits.
+__host__ __device__ __forceinline__ uint32_t digit_mask(int key_bits, int p) {
+    int left = key_bits - 8 * p;
+    return left >= 8 ? 0xffu : ((1u << left) - 1u);
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(const uint64_t *__restrict__ keys, uint32_t n, int key_bits,
                                                     uint32_t *__restrict__ hist) {
+    const int passes = (key_bits + 7) / 8;
     __shared__ uint32_t sh[8][kRadix];
     for (int i = threadIdx.x; i < 8 * kRadix; i += blockDim.x) (&sh[0][0])[i] = 0u;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint64_t k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 0xffu], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & digit_mask(key_bits, p)], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
@@ -80,7 +87,7 @@ __device__ __forceinline__ uint32_t block_scan256(uint32_t v, uint32_t *s_warp, 
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__restrict__ kin,
                                                             const uint32_t *__restrict__ vin,
                                                             uint64_t *__restrict__ kout,
-                                                            uint32_t *__restrict__ vout, uint32_t n, int shift,
+                                                            uint32_t *__restrict__ vout, uint32_t n, int shift, uint32_t dmask,
                                                             const uint32_t *__restrict__ hist,
                                                             uint32_t *__restrict__ status,
                                                             uint32_t *__restrict__ tile_counter, uint32_t *err) {
@@ -117,7 +124,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
         uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
         bool valid = idx < n;
         uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-        uint32_t d = (uint32_t)(k[j] >> shift) & 0xffu;
+        uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
         uint32_t old = 0, below = 0;
         int leader = lane;
         if (valid) {
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
     for (int j = 0; j < kSortItems; ++j) {
         uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
         if (idx < n) {
-            uint32_t d = (uint32_t)(k[j] >> shift) & 0xffu;
+            uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
             uint32_t pos = s_digit_excl[d] + s_whist[w * kRadix + d] + rank[j];
             s_keys[pos] = k[j];
             s_vals[pos] = v[j];
@@ -193,7 +200,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
     const uint32_t tile_n = (n - base) < (uint32_t)kSortTile ? (n - base) : (uint32_t)kSortTile;
     for (uint32_t i = (uint32_t)t; i < tile_n; i += kSortThreads) {
         uint64_t key = s_keys[i];
-        uint32_t d = (uint32_t)(key >> shift) & 0xffu;
+        uint32_t d = (uint32_t)(key >> shift) & dmask;
         uint32_t o = s_global[d] + (i - s_digit_excl[d]);
         if (o < n) {
             kout[o] = key;
@@ -219,8 +226,9 @@ uint64_t sort_scratch_bytes(uint32_t n, int passes) {
 // keys0/vals0.  `keys_hist_done`: the caller already accumulated the digit
 // histograms into the scratch (fused with key generation).
 int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
-               uint32_t *vals1, uint32_t n, int passes, void *scratch, bool hist_done, uint32_t *err) {
+               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err) {
     if (n == 0) return RT_OK;
+    const int passes = (key_bits + 7) / 8;
     if (n > kValueMask) return RT_ERR_UNSUPPORTED;
     uint8_t *s = static_cast<uint8_t *>(scratch);
     uint32_t *hist = reinterpret_cast<uint32_t *>(s);
@@ -234,7 +242,7 @@ int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint
         int blocks = (int)((n + 255u) / 256u);
         int cap = ctx->sm_count * 8;
         if (blocks > cap) blocks = cap;
-        k_sort_hist<<<blocks, 256, 0, stream>>>(keys0, n, passes, hist);
+        k_sort_hist<<<blocks, 256, 0, stream>>>(keys0, n, key_bits, hist);
         RT_CUDA_TRY(cudaGetLastError());
     }
     RT_CUDA_TRY(cudaMemsetAsync(counters, 0, 8u * 4u, stream));
@@ -247,7 +255,7 @@ int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint
         uint64_t *ko = (p & 1) ? keys0 : keys1;
         uint32_t *vo = (p & 1) ? vals0 : vals1;
         k_onesweep<<<(unsigned)tiles, kSortThreads, kSortSmemBytes, stream>>>(
-            ki, vi, ko, vo, n, 8 * p, hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err);
+            ki, vi, ko, vo, n, 8 * p, digit_mask(key_bits, p), hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err);
         RT_CUDA_TRY(cudaGetLastError());
     }
     if (passes & 1) {
@@ -283,7 +291,7 @@ extern "C" rt_status rt_sort_pairs(rt_context *ctx, rt_stream stream, uint64_t *
     uint64_t *k1 = reinterpret_cast<uint64_t *>(s);
     uint32_t *v1 = reinterpret_cast<uint32_t *>(s + (size_t)n * 8u);
     void *sort_s = s + rtc::align_up((uint64_t)n * 12u, 256);
-    int st = rtc::sort_pairs(ctx, static_cast<cudaStream_t>(stream), keys, vals, k1, v1, n, passes, sort_s, false,
+    int st = rtc::sort_pairs(ctx, static_cast<cudaStream_t>(stream), keys, vals, k1, v1, n, (int)key_bits, sort_s, false,
                              ctx->d_err);
     if (st) return rtc::set_error(ctx, st, "rt_sort_pairs: launch failed");
     return RT_OK;
