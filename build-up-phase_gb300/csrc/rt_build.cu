@@ -980,3 +980,99 @@ extern "C" rt_status rt_debug_blas_scratch_layout(uint32_t n_tris, uint32_t flag
     if (bin_off) *bin_off = L.bin;
     return RT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Bottom-level build that allocates nothing
+// ---------------------------------------------------------------------------
+//
+// Callers that cannot allocate device memory -- a plugin that only receives
+// buffers from the engine that owns all device memory, or a frame loop that
+// may not call cudaMalloc/cudaFree because they can synchronise the whole
+// device and stall the work other streams have in flight -- still need a
+// build scratch area.  This entry point uses a fixed scratch array compiled
+// into the library instead of a caller buffer.
+//
+// The array lives in device memory of every GPU that loads the library, from
+// module load until the process exits.  Host code may not use its name as a
+// device address (on the host it names a stand-in object), so the device
+// address is fetched once per device with cudaGetSymbolAddress, with that
+// device current, by the first call on that device; that first call should
+// therefore come before any stream capture.  All calls share the one array:
+// two calls whose work overlaps on the GPU (different streams, no ordering
+// between them) race on it and both results are undefined.  Each build
+// clears, on its stream, every part of the scratch that must start at zero
+// (centroid bounds, sort histograms, look-back status, refit counters), so
+// what an earlier call left there does not matter.
+
+namespace rtc {
+namespace {
+
+constexpr uint64_t kStaticScratchBytes = 32ull << 20;  // 32 MiB per device
+constexpr int kStaticScratchDevices = 64;
+
+__device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
+
+void *g_static_scratch_addr[kStaticScratchDevices] = {};
+
+// Device address of g_static_scratch on ctx->device (looked up once).
+int static_scratch_address(rt_context *ctx, void **out) {
+    if (ctx->device < 0 || ctx->device >= kStaticScratchDevices)
+        return set_error(ctx, RT_ERR_UNSUPPORTED, "static scratch: device ordinal beyond 63");
+    void *p = __atomic_load_n(&g_static_scratch_addr[ctx->device], __ATOMIC_ACQUIRE);
+    if (!p) {
+        int cur = -1;
+        RT_CUDA_CTX(ctx, cudaGetDevice(&cur));
+        if (cur != ctx->device) RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (cur != ctx->device) cudaSetDevice(cur);
+        if (e != cudaSuccess) return set_cuda_error(ctx, e, "cudaGetSymbolAddress(g_static_scratch)");
+        __atomic_store_n(&g_static_scratch_addr[ctx->device], p, __ATOMIC_RELEASE);
+    }
+    *out = p;
+    return RT_OK;
+}
+
+}  // namespace
+}  // namespace rtc
+
+extern "C" rt_status rt_build_blas_static_scratch(rt_context *ctx, rt_stream stream,
+                                                  const rt_geometry_triangles *geoms, uint32_t n_geoms,
+                                                  uint32_t flags, void *accel, uint64_t accel_bytes) {
+    if (!ctx || !accel || (n_geoms && !geoms))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas_static_scratch: null argument");
+    if (n_geoms > (uint32_t)kMaxGeoms)
+        return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 256 geometries in one BLAS");
+    if ((flags & RT_BUILD_MORTON30) && (flags & RT_BUILD_MORTON63))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_MORTON30 and RT_BUILD_MORTON63 are exclusive");
+    static thread_local GeomParams gp;
+    std::memset(&gp, 0, sizeof(gp));
+    gp.n_geoms = n_geoms;
+    uint64_t total = 0;
+    for (uint32_t g = 0; g < n_geoms; ++g) {
+        const rt_geometry_triangles &G = geoms[g];
+        if (G.tri_count && (!G.vertices || G.vertex_stride < 12u ||
+                            (G.index_type != RT_INDEX_UINT32 && G.index_type != RT_INDEX_NONE) ||
+                            (G.index_type == RT_INDEX_UINT32 && !G.indices)))
+            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas_static_scratch: bad geometry descriptor");
+        if (G.index_type == RT_INDEX_NONE && G.tri_count && (uint64_t)G.tri_count * 3u - 1u > G.max_vertex)
+            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas_static_scratch: non-indexed geometry exceeds max_vertex");
+        gp.table[g] = (uint32_t)total;
+        gp.g[g] = G;
+        total += G.tri_count;
+    }
+    if (total > RT_STATIC_SCRATCH_MAX_TRIS)
+        return set_error(ctx, RT_ERR_UNSUPPORTED,
+                         "rt_build_blas_static_scratch: more than RT_STATIC_SCRATCH_MAX_TRIS (131072) triangles; "
+                         "use rt_build_blas with a caller-allocated scratch buffer");
+    gp.table[n_geoms] = (uint32_t)total;
+    const int passes = (flags & RT_BUILD_MORTON30) ? 4 : 8;
+    const BuildLayout L = build_layout((uint32_t)total, 48u, passes);
+    if (L.total > kStaticScratchBytes)
+        return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_build_blas_static_scratch: scratch layout exceeds the static array");
+    void *scratch = nullptr;
+    int rc = static_scratch_address(ctx, &scratch);
+    if (rc) return rc;
+    BuildCall bc{RT_ACCEL_KIND_BLAS, (uint32_t)total, 48u, n_geoms, flags};
+    return run_build(ctx, static_cast<cudaStream_t>(stream), bc, &gp, nullptr, accel, accel_bytes, scratch,
+                     kStaticScratchBytes, nullptr);
+}

@@ -49,6 +49,7 @@ RT_CHIT_SAMPLE = 0
 RT_CHIT_BARYCENTRIC = 1
 RT_CHIT_SBT_COLOR = 2
 RT_NO_HIT = 0xFFFFFFFF
+RT_STATIC_SCRATCH_MAX_TRIS = 131072
 RT_GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE = 1
 
 
@@ -117,6 +118,7 @@ PROTOTYPES = {
     "rt_get_tlas_build_sizes": (_i32, [_vp, _u32, _u32, C.POINTER(BuildSizes)]),
     "rt_build_blas": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _u32, _vp, _u64, _vp, _u64]),
     "rt_build_tlas": (_i32, [_vp, _vp, _vp, _u32, _u32, _vp, _u64, _vp, _u64]),
+    "rt_build_blas_static_scratch": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _u32, _vp, _u64]),
     "rt_accel_address": (_u64, [_vp]),
     "rt_accel_info": (_i32, [_vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "rt_trace_rays": (_i32, [_vp, _vp, C.POINTER(Pipeline), C.POINTER(Sbt), _u64, C.POINTER(Camera), _vp,
@@ -232,6 +234,13 @@ class Context:
         arr = (GeometryTriangles * max(1, len(geoms)))(*geoms)
         self.check(self.lib.rt_build_blas(self.h, _stream_ptr(stream), arr, len(geoms), flags, _ptr(accel),
                                           accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_blas")
+
+    def build_blas_static_scratch(self, geoms, flags, accel, accel_bytes, stream=None) -> None:
+        """rt_build_blas_static_scratch: the build without a caller scratch
+        buffer (at most RT_STATIC_SCRATCH_MAX_TRIS triangles)."""
+        arr = (GeometryTriangles * max(1, len(geoms)))(*geoms)
+        self.check(self.lib.rt_build_blas_static_scratch(self.h, _stream_ptr(stream), arr, len(geoms), flags,
+                                                         _ptr(accel), accel_bytes), "rt_build_blas_static_scratch")
 
     def build_tlas(self, instances, n, flags, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
         self.check(self.lib.rt_build_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, flags, _ptr(accel),

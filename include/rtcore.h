@@ -240,6 +240,30 @@ rt_status rt_build_blas(rt_context *ctx, rt_stream stream,
                         void *scratch, uint64_t scratch_bytes);
 
 /*
+ * rt_build_blas without a scratch buffer, for callers that cannot allocate
+ * device memory: for instance a plugin that is handed its input and output
+ * buffers by an engine that owns all device memory, or a frame loop that must
+ * not call cudaMalloc/cudaFree because they can synchronise the device and
+ * stall other streams.  This call itself allocates nothing.  It has no
+ * counterpart in the reference (whose Vulkan sample allocates its scratch
+ * buffer with vkAllocateMemory).
+ *
+ * The scratch is one fixed 32 MiB array compiled into the library, held in
+ * device memory of every GPU that loads the library until the process
+ * exits; it limits a build to RT_STATIC_SCRATCH_MAX_TRIS triangles (larger
+ * inputs return RT_ERR_UNSUPPORTED -- use rt_build_blas).  The first call on
+ * each device looks up the array's device address, so make that first call
+ * before any stream capture.  Every call shares the array: calls whose work
+ * overlaps on the GPU race and give undefined results; order them on one
+ * stream (or with events).  Output is byte-identical to rt_build_blas.
+ */
+#define RT_STATIC_SCRATCH_MAX_TRIS 131072u
+rt_status rt_build_blas_static_scratch(rt_context *ctx, rt_stream stream,
+                                       const rt_geometry_triangles *geoms,
+                                       uint32_t n_geoms, uint32_t flags,
+                                       void *accel, uint64_t accel_bytes);
+
+/*
  * vkCmdBuildAccelerationStructuresKHR for one top-level structure
  * (main.cpp:920-940).  `instances` is a device array of n rt_instance whose
  * accel_ref fields point at completed bottom-level builds.
