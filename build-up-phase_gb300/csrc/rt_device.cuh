@@ -176,16 +176,37 @@ __device__ __forceinline__ NodeWords load_node(const uint4 *nodes, uint32_t idx)
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xffu; }
 
+// Byte b of w as an exact float: PRMT assembles 0x4B0000qq (= 2^23 + q) and
+// one FADD removes 2^23.  Same value as (float)q without the conversion pipe.
+__device__ __forceinline__ float qbyte(uint32_t w, int b) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)b)) - 8388608.0f;
+}
+
+// Three-input min/max (sm_100+ PTX); exact, so equal to two-input chains.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Box test of a node's 8 children against [tmin, tcur].
 //   node_hits: bit (slot ^ oct) for every internal child hit
 //   prim_hits: leaf-record mask relative to the node's prim_base
+// An internal child's meta byte is 0x20 | (24 + slot) and a leaf's offset is
+// below 24, so XOR-ing the octant into the internal bytes (four at a time)
+// lets one shift-or per hit slot build both masks: internal children land on
+// bit 24 + (slot ^ oct), leaf records on their offsets.
 __device__ __forceinline__ void isect_node(const Ray &r, const NodeWords &n, float tmin, float tcur,
                                            uint32_t &node_hits, uint32_t &prim_hits) {
     const float px = __uint_as_float(n.w0.x), py = __uint_as_float(n.w0.y), pz = __uint_as_float(n.w0.z);
     const int ex = (int)(int8_t)(n.w0.w & 0xffu);
     const int ey = (int)(int8_t)((n.w0.w >> 8) & 0xffu);
     const int ez = (int)(int8_t)((n.w0.w >> 16) & 0xffu);
-    const uint32_t imask = n.w0.w >> 24;
     const float scx = pow2f(ex) * r.invd[0], scy = pow2f(ey) * r.invd[1], scz = pow2f(ez) * r.invd[2];
     const float adjx = (px - r.o[0]) * r.invd[0];
     const float adjy = (py - r.o[1]) * r.invd[1];
@@ -195,33 +216,30 @@ __device__ __forceinline__ void isect_node(const Ray &r, const NodeWords &n, flo
     const uint32_t hix[2] = {n.w3.z, n.w3.w}, hiy[2] = {n.w4.x, n.w4.y}, hiz[2] = {n.w4.z, n.w4.w};
     const uint32_t meta[2] = {n.w1.z, n.w1.w};
     const bool nx = r.oct & 1u, ny = r.oct & 2u, nz = r.oct & 4u;
-    uint32_t nh = 0, ph = 0;
+    uint32_t hits = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const uint32_t nearx = nx ? hix[h] : lox[h], farx = nx ? lox[h] : hix[h];
         const uint32_t neary = ny ? hiy[h] : loy[h], fary = ny ? loy[h] : hiy[h];
         const uint32_t nearz = nz ? hiz[h] : loz[h], farz = nz ? loz[h] : hiz[h];
+        const uint32_t inner4 = (meta[h] >> 3) & (meta[h] >> 4) & 0x01010101u;
+        const uint32_t mx4 = meta[h] ^ (inner4 * r.oct);
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const int s = 4 * h + b;
-            float tn = fmaxf(fmaxf(fmaxf(tmin, __fmaf_rn((float)byte_of(nearx, b), scx, adjx)),
-                                   __fmaf_rn((float)byte_of(neary, b), scy, adjy)),
-                             __fmaf_rn((float)byte_of(nearz, b), scz, adjz));
-            float tf = fminf(fminf(fminf(tcur, __fmaf_rn((float)byte_of(farx, b), scx, adjx)),
-                                   __fmaf_rn((float)byte_of(fary, b), scy, adjy)),
-                             __fmaf_rn((float)byte_of(farz, b), scz, adjz));
+            const float tn = fmaxf(fmax3(tmin, __fmaf_rn(qbyte(nearx, b), scx, adjx),
+                                         __fmaf_rn(qbyte(neary, b), scy, adjy)),
+                                   __fmaf_rn(qbyte(nearz, b), scz, adjz));
+            const float tf = fminf(fmin3(tcur, __fmaf_rn(qbyte(farx, b), scx, adjx),
+                                         __fmaf_rn(qbyte(fary, b), scy, adjy)),
+                                   __fmaf_rn(qbyte(farz, b), scz, adjz));
             if (tn <= tf * kTfarScale) {
-                if (imask & (1u << s)) {
-                    nh |= 1u << ((uint32_t)s ^ r.oct);
-                } else {
-                    const uint32_t m = byte_of(meta[h], b);
-                    ph |= (m >> 5) << (m & 31u);
-                }
+                const uint32_t m = byte_of(mx4, b);
+                hits |= (m >> 5) << (m & 31u);
             }
         }
     }
-    node_hits = nh;
-    prim_hits = ph;
+    node_hits = hits >> 24;
+    prim_hits = hits & 0x00ffffffu;
 }
 
 // Device-side error reporting: the first error code wins.

@@ -258,7 +258,7 @@ struct BatchArgs {
 };
 
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_blas(const BatchArgs a) {
+__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_blas(const BatchArgs a) {
     __shared__ uint2 s_stack[kRing][kTraceThreads];
     const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
     const uint4 *nodes = reinterpret_cast<const uint4 *>(a.accel + hd->node_offset);
@@ -564,7 +564,7 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     a.hits_ext = hits_ext;
     a.occluded = occ;
     a.n = n;
-    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 8u;
+    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 4u;
     if (a.refill > 32u) a.refill = 32u;
     a.err = ctx->d_err;
     a.stats = stats;
