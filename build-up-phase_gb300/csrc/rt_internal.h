@@ -2,6 +2,7 @@
 // librtcore: the context object, error plumbing and cross-file launchers.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -41,6 +42,19 @@ int set_cuda_error(rt_context *ctx, cudaError_t e, const char *where);
 
 // Next work counter (zeroed on `stream` before it is handed out).
 uint32_t *acquire_counter(rt_context *ctx, cudaStream_t stream);
+
+// aspect_y = tan(radians(yFov) * 0.5), aspect_x = aspect_y * W / H of the
+// sample's raygen (main.cpp:1039-1040): radians and the halving in float as
+// GLSL evaluates them, tan in double rounded once, on the host.
+inline void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *ay, float *ax) {
+    const float half = (cam->y_fov_degree * (float)(3.14159265358979323846 / 180.0)) * 0.5f;
+    *ay = (float)std::tan((double)half);
+    *ax = (*ay * (float)w) / (float)h;
+}
+
+// Queue-driven BLAS traversal (rt_trace.cu) used by the path tracer.
+int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
+                       uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any);
 
 // Sort (rt_sort.cu)
 uint64_t sort_scratch_bytes(uint32_t n, int passes);

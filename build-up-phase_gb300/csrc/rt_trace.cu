@@ -255,6 +255,8 @@ struct BatchArgs {
     uint32_t *counter;
     uint32_t *err;
     unsigned long long *stats;
+    const uint32_t *n_dev;   // when set: the ray count, read on the device
+    uint32_t out_rec;        // closest hit: write the leaf-record index
 };
 
 template <bool ANY, bool STATS>
@@ -283,6 +285,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_blas(const BatchArgs
     // past the end, can only come from a corrupt structure.
     const uint32_t max_visits = hd->node_count;
     uint32_t visits = 0;
+    const uint32_t n_rays = a.n_dev ? min(*a.n_dev, a.n) : a.n;
 
     for (;;) {
         // ---- refill idle lanes from the global counter
@@ -292,10 +295,10 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_blas(const BatchArgs
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(a.counter, cnt);
             base = __shfl_sync(0xffffffffu, base, 0);
-            if (base + cnt >= a.n) exhausted = true;
+            if (base + cnt >= n_rays) exhausted = true;
             if (!active) {
                 const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
-                if (idx < a.n) {
+                if (idx < n_rays) {
                     const float4 r0 = __ldg(a.rays + 2u * idx), r1 = __ldg(a.rays + 2u * idx + 1u);
                     const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
                     ray_setup(r, o, d);
@@ -398,7 +401,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_blas(const BatchArgs
                         if (a.occluded) a.occluded[ray_idx] = h.found ? 1u : 0u;
                     } else {
                         float4 out;
-                        if (h.found) out = make_float4(h.t, __uint_as_float(h.tri), h.u, h.v);
+                        if (h.found) out = make_float4(h.t, __uint_as_float(a.out_rec ? h.rec : h.tri), h.u, h.v);
                         else out = make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
                         if (a.hits) a.hits[ray_idx] = out;
                         if (a.hits_ext) {
@@ -568,6 +571,8 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     if (a.refill > 32u) a.refill = 32u;
     a.err = ctx->d_err;
     a.stats = stats;
+    a.n_dev = nullptr;
+    a.out_rec = 0;
     a.counter = acquire_counter(ctx, st);
     if (!a.counter) return set_error(ctx, RT_ERR_CUDA, "work counter reset failed");
     uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
@@ -598,13 +603,42 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     return RT_OK;
 }
 
-void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *ay, float *ax) {
-    // aspect_y = tan(radians(yFov) * 0.5) (main.cpp:1039): radians and the
-    // halving in float as GLSL evaluates them, tan in double rounded once.
-    const float half = (cam->y_fov_degree * (float)(3.14159265358979323846 / 180.0)) * 0.5f;
-    *ay = (float)std::tan((double)half);
-    *ax = (*ay * (float)w) / (float)h;
+}  // namespace
+
+// Queue-driven BLAS traversal for the wavefront path tracer: the ray count is
+// read on the device from *n_dev (at most max_n), the work counter is
+// `counter` (zeroed by the caller on the stream), and closest hits carry the
+// leaf-record index.  Capturable in a CUDA graph (no host reads, no
+// allocation).
+int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
+                       uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any) {
+    if (max_n == 0) return RT_OK;
+    BatchArgs a;
+    a.accel = accel;
+    a.rays = static_cast<const float4 *>(rays);
+    a.hits = static_cast<float4 *>(hits);
+    a.hits_ext = nullptr;
+    a.occluded = occluded;
+    a.n = max_n;
+    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 4u;
+    if (a.refill > 32u) a.refill = 32u;
+    a.err = ctx->d_err;
+    a.stats = nullptr;
+    a.n_dev = n_dev;
+    a.out_rec = 1;
+    a.counter = counter;
+    uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
+    uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
+    uint32_t need = (max_n + kTraceThreads - 1) / kTraceThreads;
+    if (blocks > need) blocks = need;
+    if (any) k_trace_blas<true, false><<<blocks, kTraceThreads, 0, st>>>(a);
+    else k_trace_blas<false, false><<<blocks, kTraceThreads, 0, st>>>(a);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
 }
+
+namespace {
+
 
 }  // namespace
 }  // namespace rtc

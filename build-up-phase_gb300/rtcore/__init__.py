@@ -102,6 +102,22 @@ class TraceTuning(C.Structure):
                 ("batch_rays", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class PtLight(C.Structure):
+    _fields_ = [("v0", C.c_float * 3), ("v1", C.c_float * 3), ("v2", C.c_float * 3), ("emission", C.c_float * 3)]
+
+
+class PtScene(C.Structure):
+    _fields_ = [("accel", C.c_uint64), ("tri_material", C.c_void_p), ("materials", C.c_void_p),
+                ("n_materials", C.c_uint32), ("lights", C.c_void_p), ("n_lights", C.c_uint32)]
+
+
+class PtParams(C.Structure):
+    _fields_ = [("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("sample_offset", C.c_uint32), ("max_depth", C.c_uint32), ("rr_depth", C.c_uint32),
+                ("seed", C.c_uint64), ("ray_eps", C.c_float), ("flags", C.c_uint32)]
+
+
+assert C.sizeof(PtLight) == 48
 assert C.sizeof(GeometryTriangles) == 48
 assert C.sizeof(Instance) == 64
 assert C.sizeof(Camera) == 16
@@ -135,6 +151,10 @@ PROTOTYPES = {
     "rt_get_sort_scratch_bytes": (_i32, [_u32, _u32, C.POINTER(_u64)]),
     "rt_sort_pairs": (_i32, [_vp, _vp, _vp, _vp, _u32, _u32, _vp, _u64]),
     "rt_debug_blas_scratch_layout": (_i32, [_u32, _u32, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    # path tracer declared in include/rtcore_pt.h
+    "rt_pt_scratch_bytes": (_i32, [C.POINTER(PtParams), C.POINTER(_u64)]),
+    "rt_path_trace": (_i32, [_vp, _vp, C.POINTER(PtScene), C.POINTER(PtParams), _vp, _vp, _u64]),
+    "rt_pt_ray_counts": (_i32, [_vp, _vp, C.POINTER(PtParams), _u32, _vp, C.POINTER(_u64), C.POINTER(_u64)]),
     # seeded scenes declared in include/rtcore_scene.h (host code)
     "rt_scene_soup": (_i32, [_u64, _u32, _vp, _vp]),
     "rt_scene_box_counts": (_i32, [_u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
@@ -290,6 +310,22 @@ class Context:
         t = TraceTuning()
         self.check(self.lib.rt_get_trace_tuning(self.h, C.byref(t)), "rt_get_trace_tuning")
         return t
+
+    # ---- path tracer
+    def pt_scratch_bytes(self, params: PtParams) -> int:
+        out = C.c_uint64()
+        self.check(self.lib.rt_pt_scratch_bytes(C.byref(params), C.byref(out)), "rt_pt_scratch_bytes")
+        return out.value
+
+    def path_trace(self, scene: PtScene, params: PtParams, accum, scratch, scratch_bytes: int, stream=None) -> None:
+        self.check(self.lib.rt_path_trace(self.h, _stream_ptr(stream), C.byref(scene), C.byref(params), _ptr(accum),
+                                          _ptr(scratch), scratch_bytes), "rt_path_trace")
+
+    def pt_ray_counts(self, params: PtParams, n_lights: int, scratch, stream=None):
+        e, s = C.c_uint64(), C.c_uint64()
+        self.check(self.lib.rt_pt_ray_counts(self.h, _stream_ptr(stream), C.byref(params), n_lights, _ptr(scratch),
+                                             C.byref(e), C.byref(s)), "rt_pt_ray_counts")
+        return e.value, s.value
 
     # ---- utilities
     def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:

@@ -88,3 +88,22 @@ TRI1_VERTICES = np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], np.float32)
 TRI1_INDICES = np.array([[0, 1, 2]], np.uint32)
 TRI1_CAMERA = ((0.0, 0.0, 2.5), 60.0)
 TRI1_SIZE = (800, 600)
+
+# rt_pt_light: three vertices and the emitted radiance (48 bytes)
+LIGHT_DTYPE = np.dtype([("v0", "<f4", 3), ("v1", "<f4", 3), ("v2", "<f4", 3), ("emission", "<f4", 3)])
+
+# The box workload's path-tracing setup: camera inside the box near the front
+# wall, looking -z with the sample's raygen basis.
+BOX_CAMERA = ((0.0, 0.0, 0.95), 60.0)
+
+
+def emissive_lights(v: np.ndarray, i: np.ndarray, tri_material: np.ndarray, materials: np.ndarray) -> np.ndarray:
+    """Every triangle whose material emits, as rt_pt_light records."""
+    em = materials["emission"][tri_material]
+    sel = np.nonzero((em > 0).any(axis=1))[0]
+    out = np.zeros(len(sel), LIGHT_DTYPE)
+    out["v0"] = v[i[sel, 0]]
+    out["v1"] = v[i[sel, 1]]
+    out["v2"] = v[i[sel, 2]]
+    out["emission"] = em[sel]
+    return out

@@ -1,0 +1,76 @@
+/*
+ * rtcore_pt.h -- wavefront path tracer of the GB300 ray-tracing core.
+ *
+ * No counterpart in the reference: its sample shades one bounce with a
+ * constant closest-hit colour (vulkan-raytraced-triangle/main.cpp:1080-1091).
+ * The path tracer reuses the sample's pinhole camera model (main.cpp:1036-1045)
+ * with a per-sample sub-pixel jitter, and traces with the same BVH8 kernels.
+ *
+ * Light transport: Lambertian surfaces, next-event estimation to emissive
+ * triangles (area sampling), one-sided emitters (along the triangle's
+ * geometric normal, (v1-v0) x (v2-v0)), Russian roulette from rr_depth on,
+ * at most max_depth path vertices.  Random numbers: one PCG32 stream per pixel
+ * and sample (state seeded from the sample index, stream = pixel index), six
+ * draws per path vertex (light pick, 2 for the light point, 2 for the BSDF,
+ * roulette) and two for the camera jitter, consumed whether used or not.
+ */
+#ifndef RTCORE_PT_H
+#define RTCORE_PT_H
+
+#include "rtcore.h"
+#include "rtcore_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* An emissive triangle for next-event estimation (48 bytes). */
+typedef struct rt_pt_light {
+    float v0[3], v1[3], v2[3];
+    float emission[3];
+} rt_pt_light;
+
+typedef struct rt_pt_scene {
+    uint64_t accel;                 /* bottom-level rt_accel_address        */
+    const uint32_t *tri_material;   /* device, material of each build-input
+                                       triangle                            */
+    const rt_material *materials;   /* device                               */
+    uint32_t n_materials;
+    const rt_pt_light *lights;      /* device                               */
+    uint32_t n_lights;
+} rt_pt_scene;
+
+typedef struct rt_pt_params {
+    rt_camera camera;
+    uint32_t width, height;
+    uint32_t spp;            /* samples per pixel traced by this call        */
+    uint32_t sample_offset;  /* index of the first sample (progressive use) */
+    uint32_t max_depth;      /* path vertices, >= 1                          */
+    uint32_t rr_depth;       /* Russian roulette from this vertex index on   */
+    uint64_t seed;
+    float ray_eps;           /* secondary-ray offset along the normal        */
+    uint32_t flags;          /* 0                                            */
+} rt_pt_params;
+
+/* Scratch bytes of rt_path_trace for these parameters. */
+rt_status rt_pt_scratch_bytes(const rt_pt_params *p, uint64_t *bytes);
+
+/*
+ * Traces p->spp samples per pixel and ADDS them to accum (device,
+ * width*height*4 floats, row-major): rgb += sum of sample radiances,
+ * a += number of samples.  Zero accum before the first call; divide rgb by a
+ * to resolve.  Asynchronous on `stream`.
+ */
+rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene, const rt_pt_params *p,
+                        float *accum, void *scratch, uint64_t scratch_bytes);
+
+/* Extension rays (camera + bounce) and shadow rays traced by the last
+ * rt_path_trace call that used `scratch` with these parameters and light
+ * count (synchronises `stream`). */
+rt_status rt_pt_ray_counts(rt_context *ctx, rt_stream stream, const rt_pt_params *p, uint32_t n_lights,
+                           const void *scratch, uint64_t *extension_rays, uint64_t *shadow_rays);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

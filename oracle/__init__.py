@@ -18,8 +18,7 @@ REPO = HERE.parent
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
 SRC = [HERE / "oracle.cpp"]
-DEPS = SRC + [HERE / "oracle.h", REPO / "include" / "rtcore.h", REPO / "include" / "rtcore_accel.h",
-              Path(__file__)]
+DEPS = SRC + [HERE / "oracle.h", Path(__file__)] + sorted((REPO / "include").glob("*.h"))
 
 # -ffp-contract=off: one rounding per operation, as the GPU kernels
 # (-fmad=false); no -march flags so x86-64 and aarch64 round alike.
@@ -62,6 +61,8 @@ def load() -> C.CDLL:
         "orc_trace_rays": (i32, [vp, vp, u32, u32, vp, vp, vp, u32, u32, u32]),
         "orc_sort_pairs": (None, [vp, vp, u32, u32]),
         "orc_hw_threads": (u32, []),
+        "orc_path_trace": (i32, [vp, vp, vp, u32, vp, u32, vp, vp, u32]),
+        "orc_sincos_q": (None, [f, vp, vp]),
     }
     for name, (res, args) in protos.items():
         fn = getattr(lib, name)
@@ -269,6 +270,38 @@ def sort_pairs(keys: np.ndarray, vals: np.ndarray, bits: int):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     lib.orc_sort_pairs(k.ctypes.data, v.ctypes.data, len(k), bits)
     return k, v
+
+
+class _PtParams(C.Structure):
+    _fields_ = [("camera", _Camera), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("sample_offset", C.c_uint32), ("max_depth", C.c_uint32), ("rr_depth", C.c_uint32),
+                ("seed", C.c_uint64), ("ray_eps", C.c_float), ("flags", C.c_uint32)]
+
+
+def path_trace(accel: np.ndarray, tri_material: np.ndarray, materials: np.ndarray, lights: np.ndarray, camera,
+               width: int, height: int, spp: int, max_depth: int = 8, rr_depth: int = 3, seed: int = 0,
+               eps: float = 1e-4, sample_offset: int = 0, accum: np.ndarray | None = None, threads: int = 0):
+    """rt_path_trace on the CPU; returns the accumulation buffer
+    (float32 [H, W, 4]: radiance sums, sample count)."""
+    lib = load()
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    tm = np.ascontiguousarray(tri_material, np.uint32)
+    mats = np.ascontiguousarray(materials)
+    lts = np.ascontiguousarray(lights)
+    p = _PtParams(_Camera((C.c_float * 3)(*camera[0]), camera[1]), width, height, spp, sample_offset, max_depth,
+                  rr_depth, seed, eps, 0)
+    rc = lib.orc_path_trace(accel.ctypes.data, tm.ctypes.data, mats.ctypes.data, len(mats),
+                            lts.ctypes.data if len(lts) else None, len(lts), C.byref(p), accum.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_path_trace returned {rc}")
+    return accum
+
+
+def sincos_q(x: float):
+    s, c = C.c_float(), C.c_float()
+    load().orc_sincos_q(x, C.byref(s), C.byref(c))
+    return s.value, c.value
 
 
 def hw_threads() -> int:

@@ -658,6 +658,7 @@ struct HitState {
     uint64_t key;
     float u, v;
     uint32_t tri;       /* build-input triangle index */
+    uint32_t rec;       /* leaf-record index (bottom level) */
     uint32_t geom, prim;
     uint32_t inst;      /* instance index or 0 */
     uint32_t custom, sbt_off;
@@ -693,13 +694,13 @@ bool traverse_blas(const AccelView &av, const RaySetup &r, float tmin, HitState 
             uint32_t tri = fbits(rec[3]);
             uint64_t key = ((uint64_t)inst_id << 32) | tri;
             if (any_hit) {
-                hs.t = t; hs.key = key; hs.u = u; hs.v = v; hs.tri = tri;
+                hs.t = t; hs.key = key; hs.u = u; hs.v = v; hs.tri = tri; hs.rec = nd.prim_base + i;
                 hs.geom = fbits(rec[7]); hs.prim = fbits(rec[11]);
                 hs.inst = inst_id; hs.custom = custom; hs.sbt_off = sbt_off; hs.found = true;
                 return true;
             }
             if (t < hs.t || (t == hs.t && key < hs.key)) {
-                hs.t = t; hs.key = key; hs.u = u; hs.v = v; hs.tri = tri;
+                hs.t = t; hs.key = key; hs.u = u; hs.v = v; hs.tri = tri; hs.rec = nd.prim_base + i;
                 hs.geom = fbits(rec[7]); hs.prim = fbits(rec[11]);
                 hs.inst = inst_id; hs.custom = custom; hs.sbt_off = sbt_off; hs.found = true;
             }
@@ -738,6 +739,7 @@ bool traverse(const void *accel, const rt_ray &ray, HitState &hs, bool any_hit, 
     hs.found = false;
     hs.u = hs.v = 0.0f;
     hs.tri = hs.geom = hs.prim = hs.inst = hs.custom = hs.sbt_off = 0;
+    hs.rec = 0xffffffffu;
     RaySetup r;
     ray_setup(r, ray.org, ray.dir);
     if (av.h->kind == RT_ACCEL_KIND_BLAS) return traverse_blas(av, r, ray.tmin, hs, any_hit, 0, 0, 0, stats);
@@ -1118,3 +1120,219 @@ void orc_sort_pairs(uint64_t *keys, uint32_t *vals, uint32_t n, uint32_t bits) {
 }
 
 }  // extern "C"
+
+/* ====================================================================== */
+/* Path tracer (restatement of rtcore_pt.h's light transport)             */
+/* ====================================================================== */
+
+namespace {
+
+struct Rng {
+    uint64_t state, inc;
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    float uni() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }
+};
+
+uint64_t mix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+Rng rng_for(uint64_t seed, uint32_t sample, uint32_t pixel) {
+    Rng g;
+    g.inc = ((uint64_t)pixel << 1u) | 1u;
+    g.state = 0;
+    g.next();
+    g.state += mix64(seed + sample);
+    g.next();
+    return g;
+}
+
+/* Taylor polynomials of sin (to x^9) and cos (to x^8), |x| <= pi/4. */
+float poly_sin(float x) {
+    float x2 = x * x;
+    return x * (1.0f + x2 * (-1.0f / 6.0f + x2 * (1.0f / 120.0f + x2 * (-1.0f / 5040.0f + x2 * (1.0f / 362880.0f)))));
+}
+float poly_cos(float x) {
+    float x2 = x * x;
+    return 1.0f + x2 * (-0.5f + x2 * (1.0f / 24.0f + x2 * (-1.0f / 720.0f + x2 * (1.0f / 40320.0f))));
+}
+
+inline float dot(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+inline void cross(const float a[3], const float b[3], float c[3]) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+struct LightInfo {
+    float n[3];
+    float area;
+};
+
+}  // namespace
+
+extern "C" void orc_sincos_q(float x, float *s, float *c) {
+    *s = poly_sin(x);
+    *c = poly_cos(x);
+}
+
+extern "C" int orc_path_trace(const void *accel, const uint32_t *tri_material, const rt_material *materials,
+                              uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights,
+                              const rt_pt_params *p, float *accum, uint32_t n_threads) {
+    const float kInvPi = 0.318309886183790671538f, kPi4 = 0.785398163397448309616f;
+    AccelView av = view_of(accel);
+    if (av.h->kind != RT_ACCEL_KIND_BLAS) return RT_ERR_INVALID_ARG;
+    std::vector<LightInfo> li(n_lights);
+    std::vector<float> cdf(n_lights + 1);
+    float acc = 0.0f;
+    for (uint32_t k = 0; k < n_lights; ++k) {
+        const rt_pt_light &l = lights[k];
+        float e1[3], e2[3], c[3];
+        for (int a = 0; a < 3; ++a) { e1[a] = l.v1[a] - l.v0[a]; e2[a] = l.v2[a] - l.v0[a]; }
+        cross(e1, e2, c);
+        float len = std::sqrt(dot(c, c));
+        float inv = len > 0.0f ? 1.0f / len : 0.0f;
+        for (int a = 0; a < 3; ++a) li[k].n[a] = c[a] * inv;
+        li[k].area = 0.5f * len;
+        acc = acc + li[k].area;
+        cdf[k] = acc;
+    }
+    cdf[n_lights] = acc;
+    const float total = acc;
+    const float half = (p->camera.y_fov_degree * (float)(3.14159265358979323846 / 180.0)) * 0.5f;
+    const float ay = (float)std::tan((double)half);
+    const float ax = (ay * (float)p->width) / (float)p->height;
+    std::atomic<int> status{0};
+    const uint32_t npix = p->width * p->height;
+    parallel_for(npix, n_threads, [&](uint32_t b, uint32_t e) {
+        for (uint32_t pix = b; pix < e; ++pix) {
+            const uint32_t x = pix % p->width, y = pix / p->width;
+            for (uint32_t s = 0; s < p->spp; ++s) {
+                Rng g = rng_for(p->seed, p->sample_offset + s, pix);
+                float jx = g.uni(), jy = g.uni();
+                float sx = (float)x + jx, sy = (float)y + jy;
+                float ndx = (sx / (float)p->width) * 2.0f - 1.0f, ndy = (sy / (float)p->height) * 2.0f - 1.0f;
+                float pp = ndx * ax, qq = ndy * ay;
+                rt_ray ray;
+                for (int a = 0; a < 3; ++a) ray.org[a] = p->camera.position[a];
+                ray.dir[0] = (pp * 1.0f + qq * 0.0f) + 0.0f;
+                ray.dir[1] = (pp * 0.0f + qq * -1.0f) + 0.0f;
+                ray.dir[2] = (pp * 0.0f + qq * 0.0f) + -1.0f;
+                ray.tmin = 0.0f;
+                ray.tmax = 1e30f;
+                float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
+                for (uint32_t depth = 0; depth < p->max_depth; ++depth) {
+                    float u[6];
+                    for (int k = 0; k < 6; ++k) u[k] = g.uni();
+                    HitState hs;
+                    traverse(accel, ray, hs, false, 0xffu, nullptr);
+                    if (!hs.found) break;
+                    const float *rec = (const float *)(av.prims + (size_t)hs.rec * 48u);
+                    const float *v0 = rec, *v1 = rec + 4, *v2 = rec + 8;
+                    float P[3], e1[3], e2[3], ng[3], n[3];
+                    for (int a = 0; a < 3; ++a) {
+                        P[a] = ray.org[a] + hs.t * ray.dir[a];
+                        e1[a] = v1[a] - v0[a];
+                        e2[a] = v2[a] - v0[a];
+                    }
+                    cross(e1, e2, ng);
+                    float len = std::sqrt(dot(ng, ng));
+                    if (!(len > 0.0f)) break;
+                    for (int a = 0; a < 3; ++a) n[a] = ng[a] / len;
+                    float cosd = dot(n, ray.dir);
+                    uint32_t mi = tri_material[hs.tri];
+                    if (mi >= n_materials) { status = RT_ERR_BOUNDS; mi = 0; }
+                    const rt_material &m = materials[mi];
+                    if (depth == 0 && cosd < 0.0f)
+                        for (int a = 0; a < 3; ++a) L[a] = L[a] + T[a] * m.emission[a];
+                    if (cosd > 0.0f)
+                        for (int a = 0; a < 3; ++a) n[a] = -n[a];
+                    if (!(m.albedo[0] > 0.0f || m.albedo[1] > 0.0f || m.albedo[2] > 0.0f)) break;
+                    if (n_lights > 0) {
+                        float target = u[0] * total;
+                        uint32_t lo = 0, hi = n_lights - 1u;
+                        while (lo < hi) {
+                            uint32_t mid = (lo + hi) >> 1;
+                            if (cdf[mid] > target) hi = mid; else lo = mid + 1u;
+                        }
+                        const rt_pt_light &Lt = lights[lo];
+                        float su = std::sqrt(u[1]);
+                        float b0 = 1.0f - su, b1 = u[2] * su, b2 = (1.0f - b0) - b1;
+                        float lp[3], wi[3];
+                        for (int a = 0; a < 3; ++a) {
+                            lp[a] = (Lt.v0[a] * b0 + Lt.v1[a] * b1) + Lt.v2[a] * b2;
+                            wi[a] = lp[a] - P[a];
+                        }
+                        float dist2 = dot(wi, wi);
+                        float dist = std::sqrt(dist2);
+                        if (dist > 0.0f) {
+                            float wn[3];
+                            for (int a = 0; a < 3; ++a) wn[a] = wi[a] / dist;
+                            float cos_s = dot(n, wn), cos_l = -dot(li[lo].n, wn);
+                            if (cos_s > 0.0f && cos_l > 0.0f) {
+                                float f = (((cos_s * cos_l) / dist2) * total) * kInvPi;
+                                rt_ray sr;
+                                float contrib[3];
+                                for (int a = 0; a < 3; ++a) {
+                                    contrib[a] = ((T[a] * m.albedo[a]) * Lt.emission[a]) * f;
+                                    sr.org[a] = P[a] + n[a] * p->ray_eps;
+                                }
+                                for (int a = 0; a < 3; ++a) sr.dir[a] = lp[a] - sr.org[a];
+                                sr.tmin = 0.0f;
+                                sr.tmax = 0.9999f;
+                                HitState sh;
+                                if (!traverse(accel, sr, sh, true, 0xffu, nullptr))
+                                    for (int a = 0; a < 3; ++a) L[a] = L[a] + contrib[a];
+                            }
+                        }
+                    }
+                    if (depth >= p->rr_depth) {
+                        float ps = std::fmax(std::fmax(T[0], T[1]), T[2]);
+                        ps = ps < 0.95f ? ps : 0.95f;
+                        if (!(u[5] < ps)) break;
+                        for (int a = 0; a < 3; ++a) T[a] = T[a] / ps;
+                    }
+                    if (depth + 1u >= p->max_depth) break;
+                    /* cosine-weighted direction: concentric disk lifted to the hemisphere */
+                    float da = 2.0f * u[3] - 1.0f, db = 2.0f * u[4] - 1.0f, dx, dy;
+                    if (da == 0.0f && db == 0.0f) {
+                        dx = 0.0f; dy = 0.0f;
+                    } else if (std::fabs(da) > std::fabs(db)) {
+                        float phi = kPi4 * (db / da);
+                        dx = da * poly_cos(phi); dy = da * poly_sin(phi);
+                    } else {
+                        float phi = kPi4 * (da / db);
+                        dx = db * poly_sin(phi); dy = db * poly_cos(phi);
+                    }
+                    float zz = (1.0f - dx * dx) - dy * dy;
+                    float dz = std::sqrt(zz > 0.0f ? zz : 0.0f);
+                    float sign = std::copysign(1.0f, n[2]);
+                    float oa = -1.0f / (sign + n[2]);
+                    float ob = n[0] * n[1] * oa;
+                    float t1[3] = {1.0f + sign * n[0] * n[0] * oa, sign * ob, -sign * n[0]};
+                    float t2[3] = {ob, sign + n[1] * n[1] * oa, -n[1]};
+                    for (int a = 0; a < 3; ++a) {
+                        ray.dir[a] = (t1[a] * dx + t2[a] * dy) + n[a] * dz;
+                        ray.org[a] = P[a] + n[a] * p->ray_eps;
+                        T[a] = T[a] * m.albedo[a];
+                    }
+                    ray.tmin = 0.0f;
+                    ray.tmax = 1e30f;
+                }
+                float *px = accum + (size_t)pix * 4u;
+                for (int a = 0; a < 3; ++a) px[a] = px[a] + L[a];
+                px[3] = px[3] + 1.0f;
+            }
+        }
+    });
+    return status.load();
+}

@@ -22,6 +22,7 @@
 #include <stdint.h>
 #include "../include/rtcore.h"
 #include "../include/rtcore_accel.h"
+#include "../include/rtcore_pt.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -88,6 +89,16 @@ int orc_trace_rays(const rt_pipeline *p, const float *sbt_colors,
                    uint32_t sbt_count, uint32_t sbt_stride, const void *accel,
                    const rt_camera *cam, float *out_rgba32f, uint32_t width,
                    uint32_t height, uint32_t n_threads);
+
+/* The path tracer of rtcore_pt.h on the CPU, pixel by pixel: adds the
+ * samples to accum (host, width*height*4) exactly as rt_path_trace does.
+ * tri_material, materials and lights are host arrays. */
+int orc_path_trace(const void *accel, const uint32_t *tri_material, const rt_material *materials,
+                   uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights, const rt_pt_params *p,
+                   float *accum, uint32_t n_threads);
+
+/* sin and cos of the oracle's polynomial, for tests of their accuracy. */
+void orc_sincos_q(float x, float *s, float *c);
 
 /* Stable LSD radix sort of (key, value) pairs on `bits` low key bits. */
 void orc_sort_pairs(uint64_t *keys, uint32_t *vals, uint32_t n, uint32_t bits);
