@@ -11,6 +11,7 @@
 
 #include "../../include/rtcore.h"
 #include "../../include/rtcore_accel.h"
+#include "../../include/rtcore_cache.h"
 #include "rt_device.cuh"
 
 // Library-owned state of one device.  Replaces the Vulkan instance/device
@@ -55,6 +56,12 @@ inline void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *
 // Queue-driven BLAS traversal (rt_trace.cu) used by the path tracer.
 int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
                        uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any);
+
+// MLP cache launchers whose row counts live on the device (rt_mlp.cu).
+int cache_query_dev(rt_context *ctx, cudaStream_t st, const void *cache, const rt_cache_input *in, float *out,
+                    const uint32_t *n_dev, uint32_t max_n);
+int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cache_input *in, const float *targets,
+                    const uint32_t *n_dev, uint32_t max_n, uint32_t batch);
 
 // Sort (rt_sort.cu)
 uint64_t sort_scratch_bytes(uint32_t n, int passes);

@@ -1,0 +1,642 @@
+// rt_mlp.cu -- the MLP radiance cache: encoding, fused forward on the tensor
+// cores, backward, Adam.
+//
+// No counterpart in the reference (its sample has no path tracer to cache).
+//
+// Network (padded layout, FP32 master parameters and a BF16 copy):
+//   layer 0: 96 (81 used) -> 64, ReLU
+//   layers 1-4: 64 -> 64, ReLU
+//   layer 5: 64 -> 8 (3 used), linear
+// Forward: one warp owns 16 rows; each layer is m16n8k16 BF16 MMAs with FP32
+// accumulation; the FP32 accumulator fragment of one layer is exactly the
+// A-operand fragment layout of the next (after bias, ReLU and BF16 packing),
+// so activations never leave registers between layers.  Weights sit in
+// shared memory with padded row strides (bank-conflict free fragment loads).
+// Backward (training): the same MMA routine propagates delta through W^T
+// (transposed into shared memory at block start); weight gradients are FP32
+// outer products on the CUDA cores over the 64-row tile, added to global
+// FP32 gradients with atomics; Adam updates the FP32 master copy and
+// refreshes the BF16 one.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/rtcore_cache.h"
+#include "rt_internal.h"
+
+namespace rtc {
+namespace {
+
+constexpr int kLayers = 6;
+constexpr int kParams = 23368;  // sum of out*in + out
+
+__host__ __device__ constexpr int in_dim(int l) { return l == 0 ? 96 : 64; }
+__host__ __device__ constexpr int out_dim(int l) { return l == 5 ? 8 : 64; }
+__host__ __device__ constexpr int w_off(int l) {
+    int o = 0;
+    for (int k = 0; k < l; ++k) o += out_dim(k) * in_dim(k) + out_dim(k);
+    return o;
+}
+__host__ __device__ constexpr int b_off(int l) { return w_off(l) + out_dim(l) * in_dim(l); }
+static_assert(w_off(kLayers) == kParams, "parameter count");
+
+// shared-memory strides (elements): +8 bf16 keeps fragment loads conflict free
+__host__ __device__ constexpr int w_stride(int l) { return in_dim(l) + 8; }
+constexpr int kWtStride = 72;    // W^T of a 64-output layer: [in][64 + 8]
+constexpr int kWt5Stride = 24;   // W^T of the 8-output layer: [64][16 + 8]
+__host__ __device__ constexpr int sw_off(int l) {
+    int o = 0;
+    for (int k = 0; k < l; ++k) o += out_dim(k) * w_stride(k);
+    return o;
+}
+constexpr int kSwElems = sw_off(kLayers);                      // 25664
+__host__ __device__ constexpr int swt_off(int l) {               // l = 1..5
+    return (l - 1) * 64 * kWtStride;
+}
+constexpr int kSwtElems = 4 * 64 * kWtStride + 64 * kWt5Stride;  // 19968
+constexpr int kBiasFloats = 64 * 5 + 8;
+constexpr int kInStride = 104;
+constexpr int kActStride = 72;
+
+// State buffer layout (bytes)
+struct CacheState {
+    float params[kParams];
+    float grads[kParams];
+    float m[kParams];
+    float v[kParams];
+    __nv_bfloat16 wbf[kParams];
+    uint32_t step;
+    float lo[3], hi[3];
+    float lr, beta1, beta2, eps;
+    float loss;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// c[j] = bias + A (16 x 16*KS) * V^T where V is row-major [8*NT][16*KS] in
+// shared memory (stride vs).  bias may be null.
+template <int KS, int NT>
+__device__ __forceinline__ void warp_dense(const uint32_t (&a)[KS][4], const __nv_bfloat16 *V, int vs,
+                                           const float *bias, float (&c)[NT][4], int lane) {
+    const int g = lane >> 2, q = lane & 3;
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        const float b0 = bias ? bias[8 * j + 2 * q] : 0.0f, b1 = bias ? bias[8 * j + 2 * q + 1] : 0.0f;
+        c[j][0] = b0; c[j][1] = b1; c[j][2] = b0; c[j][3] = b1;
+    }
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const __nv_bfloat16 *row = V + (8 * j + g) * vs + 16 * ks + 2 * q;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + 8);
+            mma_bf16(c[j], a[ks], b0, b1);
+        }
+    }
+}
+
+// ReLU + BF16 pack of an accumulator (16 x 64) into the next layer's A
+// fragments.
+__device__ __forceinline__ void relu_to_a(const float (&c)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        a[q][0] = pack_bf16(fmaxf(c[2 * q][0], 0.0f), fmaxf(c[2 * q][1], 0.0f));
+        a[q][1] = pack_bf16(fmaxf(c[2 * q][2], 0.0f), fmaxf(c[2 * q][3], 0.0f));
+        a[q][2] = pack_bf16(fmaxf(c[2 * q + 1][0], 0.0f), fmaxf(c[2 * q + 1][1], 0.0f));
+        a[q][3] = pack_bf16(fmaxf(c[2 * q + 1][2], 0.0f), fmaxf(c[2 * q + 1][3], 0.0f));
+    }
+}
+
+// A fragments of a 16-row slab from a row-major BF16 shared-memory matrix.
+template <int KS>
+__device__ __forceinline__ void load_a(const __nv_bfloat16 *M, int ms, int r0, int lane, uint32_t (&a)[KS][4]) {
+    const int g = lane >> 2, q = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+        const __nv_bfloat16 *p0 = M + (r0 + g) * ms + 16 * ks + 2 * q;
+        const __nv_bfloat16 *p1 = p0 + 8 * ms;
+        a[ks][0] = *reinterpret_cast<const uint32_t *>(p0);
+        a[ks][1] = *reinterpret_cast<const uint32_t *>(p1);
+        a[ks][2] = *reinterpret_cast<const uint32_t *>(p0 + 8);
+        a[ks][3] = *reinterpret_cast<const uint32_t *>(p1 + 8);
+    }
+}
+
+// Input encoding of one row into 96 BF16 values.
+__device__ void encode_row(const rt_cache_input &in, const CacheState *S, __nv_bfloat16 *out) {
+    float f[96];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = S->hi[a] - S->lo[a];
+        const float pn = ext > 0.0f ? (in.pos[a] - S->lo[a]) / ext : 0.0f;
+        float scale = 1.0f;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            float s, c;
+            sincospif(scale * pn, &s, &c);
+            f[24 * a + 2 * k] = s;
+            f[24 * a + 2 * k + 1] = c;
+            scale *= 2.0f;
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        f[72 + a] = in.dir[a];
+        f[75 + a] = in.normal[a];
+        f[78 + a] = in.albedo[a];
+    }
+    for (int k = 81; k < 96; ++k) f[k] = 0.0f;
+    for (int k = 0; k < 96; k += 2)
+        *reinterpret_cast<uint32_t *>(out + k) = pack_bf16(f[k], f[k + 1]);
+}
+
+// Loads the BF16 weights (row-major, padded strides) and FP32 biases into
+// shared memory; with transpose, also W^T of layers 1..5.
+__device__ void load_weights(const CacheState *S, __nv_bfloat16 *sW, __nv_bfloat16 *sWT, float *sB) {
+    for (int l = 0; l < kLayers; ++l) {
+        const int in = in_dim(l), out = out_dim(l);
+        const __nv_bfloat16 *gw = S->wbf + w_off(l);
+        for (int e = threadIdx.x; e < out * in; e += blockDim.x) {
+            const int o = e / in, i = e % in;
+            sW[sw_off(l) + o * w_stride(l) + i] = gw[e];
+            if (sWT && l >= 1) {
+                const int st = (l == 5) ? kWt5Stride : kWtStride;
+                sWT[swt_off(l) + i * st + o] = gw[e];
+            }
+        }
+        if (sWT && l == 5)  // zero the padded k columns 8..15 of W5^T
+            for (int e = threadIdx.x; e < 64 * 16; e += blockDim.x) {
+                const int i = e / 16, k = e % 16;
+                if (k >= 8) sWT[swt_off(5) + i * kWt5Stride + k] = __float2bfloat16(0.0f);
+            }
+    }
+    for (int l = 0; l < kLayers; ++l)
+        for (int e = threadIdx.x; e < out_dim(l); e += blockDim.x) sB[(l < 5 ? 64 * l : 320) + e] = S->params[b_off(l) + e];
+}
+
+// ---------------------------------------------------------------------------
+// Inference: 128 rows per tile, 4 warps x 2 slabs of 16 rows
+// ---------------------------------------------------------------------------
+
+constexpr int kQueryRows = 128;
+constexpr size_t kQuerySmem = (size_t)kSwElems * 2 + (size_t)kBiasFloats * 4 + (size_t)kQueryRows * kInStride * 2;
+
+__global__ void __launch_bounds__(128) k_cache_query(const CacheState *S, const rt_cache_input *in, float4 *out,
+                                                     uint32_t n, const uint32_t *n_dev) {
+    if (n_dev) n = min(n, *n_dev);  // row count produced on the device
+    extern __shared__ __align__(16) uint8_t smem[];
+    __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smem);
+    float *sB = reinterpret_cast<float *>(sW + kSwElems);
+    __nv_bfloat16 *sIn = reinterpret_cast<__nv_bfloat16 *>(sB + kBiasFloats);
+    load_weights(S, sW, nullptr, sB);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, q = lane & 3;
+    const uint32_t tiles = (n + kQueryRows - 1) / kQueryRows;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        __syncthreads();  // weights loaded / previous tile done with sIn
+        const uint32_t row = tile * kQueryRows + threadIdx.x;
+        if (row < n) {
+            encode_row(in[row], S, sIn + threadIdx.x * kInStride);
+        } else {
+            for (int k = 0; k < 96; k += 2) *reinterpret_cast<uint32_t *>(sIn + threadIdx.x * kInStride + k) = 0u;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int slab = 0; slab < 2; ++slab) {
+            const int r0 = warp * 32 + slab * 16;
+            uint32_t a0[6][4];
+            load_a<6>(sIn, kInStride, r0, lane, a0);
+            float c[8][4];
+            warp_dense<6, 8>(a0, sW + sw_off(0), w_stride(0), sB, c, lane);
+            uint32_t a[4][4];
+            relu_to_a(c, a);
+#pragma unroll 1
+            for (int l = 1; l <= 4; ++l) {
+                warp_dense<4, 8>(a, sW + sw_off(l), w_stride(l), sB + 64 * l, c, lane);
+                relu_to_a(c, a);
+            }
+            float y[1][4];
+            warp_dense<4, 1>(a, sW + sw_off(5), w_stride(5), sB + 320, y, lane);
+            // y[0]: rows g / g+8, cols 2q, 2q+1 -> gather the 3 outputs of a row
+            // into one float4 store by lanes q == 0 (cols 0,1) and q == 1 (col 2)
+            const float c2_g = __shfl_sync(0xffffffffu, y[0][0], (lane & ~3) | 1);
+            const float c2_g8 = __shfl_sync(0xffffffffu, y[0][2], (lane & ~3) | 1);
+            if (q == 0) {
+                const uint32_t ra = tile * kQueryRows + r0 + g, rb = ra + 8;
+                if (ra < n) out[ra] = make_float4(y[0][0], y[0][1], c2_g, 0.0f);
+                if (rb < n) out[rb] = make_float4(y[0][2], y[0][3], c2_g8, 0.0f);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training: forward + backward over 64-row tiles, gradients into S->grads
+// ---------------------------------------------------------------------------
+
+constexpr int kTrainRows = 64;
+constexpr size_t kTrainSmem = (size_t)kSwElems * 2 + (size_t)kSwtElems * 2 + (size_t)kBiasFloats * 4 +
+                              (size_t)kTrainRows * kInStride * 2 + (size_t)5 * kTrainRows * kActStride * 2 +
+                              (size_t)kTrainRows * 64 * 4 + 64 * 4;
+
+// dW[o][i] += sum_r delta[r][o] * A[r][i] over the 64 rows; db[o] += sum_r
+// delta[r][o].  PER weights per thread (128 threads).
+template <int IN, int OUT>
+__device__ void accum_grads(const float *sD, const __nv_bfloat16 *sA, int as, float *gW, float *gb) {
+    constexpr int PER = IN * OUT / 128;
+    constexpr int TPO = IN / PER;  // threads per output row
+    const int t = threadIdx.x;
+    const int o = t / TPO, i0 = (t % TPO) * PER;
+    float acc[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) acc[k] = 0.0f;
+    for (int r = 0; r < kTrainRows; ++r) {
+        const float d = sD[r * 64 + o];
+        const __nv_bfloat16 *ar = sA + r * as + i0;
+#pragma unroll
+        for (int k = 0; k < PER; k += 2) {
+            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(ar + k);
+            acc[k] += d * __bfloat162float(v.x);
+            acc[k + 1] += d * __bfloat162float(v.y);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k)
+        if (acc[k] != 0.0f) atomicAdd(gW + o * IN + i0 + k, acc[k]);
+    if (t < OUT) {
+        float s = 0.0f;
+        for (int r = 0; r < kTrainRows; ++r) s += sD[r * 64 + t];
+        if (s != 0.0f) atomicAdd(gb + t, s);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_cache_input *in,
+                                                       const float4 *targets, uint32_t n, float inv_count,
+                                                       const uint32_t *n_dev, uint32_t row0) {
+    if (n_dev) {
+        // rows [row0, row0 + n) of a set whose size is produced on the device
+        const uint32_t total = *n_dev;
+        n = total > row0 ? min(n, total - row0) : 0u;
+        if (n == 0) return;
+        in += row0;
+        targets += row0;
+        inv_count = 1.0f / (3.0f * (float)n);
+    }
+    extern __shared__ __align__(16) uint8_t smem[];
+    __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smem);
+    __nv_bfloat16 *sWT = sW + kSwElems;
+    float *sB = reinterpret_cast<float *>(sWT + kSwtElems);
+    __nv_bfloat16 *sIn = reinterpret_cast<__nv_bfloat16 *>(sB + kBiasFloats);
+    __nv_bfloat16 *sAct = sIn + kTrainRows * kInStride;
+    float *sD = reinterpret_cast<float *>(sAct + 5 * kTrainRows * kActStride);
+    load_weights(S, sW, sWT, sB);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, q = lane & 3;
+    const int r0 = warp * 16;
+    const uint32_t tiles = (n + kTrainRows - 1) / kTrainRows;
+    float loss = 0.0f;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x < kTrainRows) {
+            const uint32_t row = tile * kTrainRows + threadIdx.x;
+            __nv_bfloat16 *dst = sIn + threadIdx.x * kInStride;
+            if (row < n) encode_row(in[row], S, dst);
+            else
+                for (int k = 0; k < 96; k += 2) *reinterpret_cast<uint32_t *>(dst + k) = 0u;
+        }
+        __syncthreads();
+        // ---- forward, keeping post-activations for the backward pass
+        uint32_t a0[6][4];
+        load_a<6>(sIn, kInStride, r0, lane, a0);
+        float c[8][4];
+        warp_dense<6, 8>(a0, sW + sw_off(0), w_stride(0), sB, c, lane);
+        uint32_t a[4][4];
+        relu_to_a(c, a);
+#pragma unroll 1
+        for (int l = 1; l <= 5; ++l) {
+            // store layer l-1 output (the input of layer l) as BF16
+            __nv_bfloat16 *act = sAct + (l - 1) * kTrainRows * kActStride;
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) {
+                *reinterpret_cast<uint32_t *>(act + (r0 + g) * kActStride + 16 * qq + 2 * q) = a[qq][0];
+                *reinterpret_cast<uint32_t *>(act + (r0 + g + 8) * kActStride + 16 * qq + 2 * q) = a[qq][1];
+                *reinterpret_cast<uint32_t *>(act + (r0 + g) * kActStride + 16 * qq + 8 + 2 * q) = a[qq][2];
+                *reinterpret_cast<uint32_t *>(act + (r0 + g + 8) * kActStride + 16 * qq + 8 + 2 * q) = a[qq][3];
+            }
+            if (l <= 4) {
+                warp_dense<4, 8>(a, sW + sw_off(l), w_stride(l), sB + 64 * l, c, lane);
+                relu_to_a(c, a);
+            }
+        }
+        float y[1][4];
+        warp_dense<4, 1>(a, sW + sw_off(5), w_stride(5), sB + 320, y, lane);
+        // ---- loss gradient at the outputs (cols 0..2 of each row)
+        float dy[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int rr = r0 + g + (e >= 2 ? 8 : 0), col = 2 * q + (e & 1);
+            const uint32_t row = tile * kTrainRows + rr;
+            dy[e] = 0.0f;
+            if (col < 3 && row < n) {
+                const float4 tg = targets[row];
+                const float yt = col == 0 ? tg.x : (col == 1 ? tg.y : tg.z);
+                const float diff = y[0][e] - yt, den = y[0][e] * y[0][e] + 0.01f;
+                dy[e] = 2.0f * diff / den * inv_count;
+                loss += diff * diff / den;
+            }
+            sD[rr * 64 + col] = dy[e];
+        }
+        uint32_t ad[4][4];
+        ad[0][0] = pack_bf16(dy[0], dy[1]);
+        ad[0][1] = pack_bf16(dy[2], dy[3]);
+        ad[0][2] = 0u;
+        ad[0][3] = 0u;
+        // ---- backward, layers 5 .. 0
+#pragma unroll 1
+        for (int L = 5; L >= 0; --L) {
+            __syncthreads();  // delta_L complete in sD
+            const __nv_bfloat16 *ain = L == 0 ? sIn : sAct + (L - 1) * kTrainRows * kActStride;
+            const int as = L == 0 ? kInStride : kActStride;
+            if (L == 5) accum_grads<64, 8>(sD, ain, as, S->grads + w_off(5), S->grads + b_off(5));
+            else if (L == 0) accum_grads<96, 64>(sD, ain, as, S->grads + w_off(0), S->grads + b_off(0));
+            else accum_grads<64, 64>(sD, ain, as, S->grads + w_off(L), S->grads + b_off(L));
+            if (L == 0) break;
+            // delta_{L-1} = (delta_L W_L) * relu'(act_{L-1})
+            float dc[8][4];
+            if (L == 5) {
+                uint32_t a1[1][4] = {{ad[0][0], ad[0][1], ad[0][2], ad[0][3]}};
+                warp_dense<1, 8>(a1, sWT + swt_off(5), kWt5Stride, nullptr, dc, lane);
+            } else {
+                warp_dense<4, 8>(ad, sWT + swt_off(L), kWtStride, nullptr, dc, lane);
+            }
+            const __nv_bfloat16 *act = sAct + (L - 1) * kTrainRows * kActStride;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const __nv_bfloat162 m0 =
+                    *reinterpret_cast<const __nv_bfloat162 *>(act + (r0 + g) * kActStride + 8 * j + 2 * q);
+                const __nv_bfloat162 m1 =
+                    *reinterpret_cast<const __nv_bfloat162 *>(act + (r0 + g + 8) * kActStride + 8 * j + 2 * q);
+                if (!(__bfloat162float(m0.x) > 0.0f)) dc[j][0] = 0.0f;
+                if (!(__bfloat162float(m0.y) > 0.0f)) dc[j][1] = 0.0f;
+                if (!(__bfloat162float(m1.x) > 0.0f)) dc[j][2] = 0.0f;
+                if (!(__bfloat162float(m1.y) > 0.0f)) dc[j][3] = 0.0f;
+            }
+            __syncthreads();  // everyone is done reading delta_L
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                sD[(r0 + g) * 64 + 8 * j + 2 * q] = dc[j][0];
+                sD[(r0 + g) * 64 + 8 * j + 2 * q + 1] = dc[j][1];
+                sD[(r0 + g + 8) * 64 + 8 * j + 2 * q] = dc[j][2];
+                sD[(r0 + g + 8) * 64 + 8 * j + 2 * q + 1] = dc[j][3];
+            }
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) {
+                ad[qq][0] = pack_bf16(dc[2 * qq][0], dc[2 * qq][1]);
+                ad[qq][1] = pack_bf16(dc[2 * qq][2], dc[2 * qq][3]);
+                ad[qq][2] = pack_bf16(dc[2 * qq + 1][0], dc[2 * qq + 1][1]);
+                ad[qq][3] = pack_bf16(dc[2 * qq + 1][2], dc[2 * qq + 1][3]);
+            }
+        }
+    }
+    // block loss -> state (mean over samples and channels)
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+    if (lane == 0) atomicAdd(&S->loss, loss * inv_count);
+}
+
+__global__ void k_cache_adam(CacheState *S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    const uint32_t t = S->step + 1u;
+    const float g = S->grads[i];
+    const float m = S->beta1 * S->m[i] + (1.0f - S->beta1) * g;
+    const float v = S->beta2 * S->v[i] + (1.0f - S->beta2) * g * g;
+    S->m[i] = m;
+    S->v[i] = v;
+    const float mh = m / (1.0f - powf(S->beta1, (float)t));
+    const float vh = v / (1.0f - powf(S->beta2, (float)t));
+    const float p = S->params[i] - S->lr * mh / (sqrtf(vh) + S->eps);
+    S->params[i] = p;
+    S->wbf[i] = __float2bfloat16(p);
+    S->grads[i] = 0.0f;
+}
+
+__global__ void k_cache_step(CacheState *S, float *loss_out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        S->step += 1u;
+        if (loss_out) *loss_out = S->loss;
+        S->loss = 0.0f;
+    }
+}
+
+__global__ void k_cache_refresh_bf16(CacheState *S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kParams) S->wbf[i] = __float2bfloat16(S->params[i]);
+}
+
+int set_smem(rt_context *ctx) {
+    RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_query, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQuerySmem));
+    RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+    return RT_OK;
+}
+
+int launch_fwd_bwd(rt_context *ctx, cudaStream_t st, CacheState *S, const rt_cache_input *in, const float *tg,
+                   uint32_t n) {
+    const uint32_t tiles = (n + kTrainRows - 1) / kTrainRows;
+    uint32_t grid = (uint32_t)ctx->sm_count;
+    if (grid > tiles) grid = tiles;
+    if (grid == 0) return RT_OK;
+    k_cache_fwd_bwd<<<grid, 128, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(tg), n,
+                                                   1.0f / (3.0f * (float)n), nullptr, 0u);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+// He-uniform initial weights of the padded layout, host side (PCG32).
+std::vector<float> initial_params(uint32_t seed) {
+    std::vector<float> p(kParams, 0.0f);
+    uint64_t state = 0, inc = ((uint64_t)seed << 1u) | 1u;
+    auto next = [&]() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u), rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    };
+    next();
+    state += 0x853c49e6748fea9bull;
+    next();
+    const int used_in[kLayers] = {RT_CACHE_INPUTS, 64, 64, 64, 64, 64};
+    const int used_out[kLayers] = {64, 64, 64, 64, 64, RT_CACHE_OUTPUTS};
+    for (int l = 0; l < kLayers; ++l) {
+        const float s = std::sqrt(6.0f / (float)used_in[l]);
+        for (int o = 0; o < used_out[l]; ++o)
+            for (int i = 0; i < used_in[l]; ++i) {
+                float u = (float)(next() >> 8) * (1.0f / 16777216.0f);
+                p[w_off(l) + o * in_dim(l) + i] = (2.0f * u - 1.0f) * s;
+            }
+    }
+    return p;
+}
+
+}  // namespace
+}  // namespace rtc
+
+using namespace rtc;
+
+extern "C" rt_status rt_cache_bytes(uint64_t *bytes) {
+    if (!bytes) return RT_ERR_INVALID_ARG;
+    *bytes = align_up(sizeof(CacheState), 256);
+    return RT_OK;
+}
+
+extern "C" uint32_t rt_cache_param_count(void) { return (uint32_t)kParams; }
+
+extern "C" rt_status rt_cache_init(rt_context *ctx, rt_stream stream, void *cache, const rt_cache_config *cfg) {
+    if (!ctx || !cache || !cfg) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_init: null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    std::vector<uint8_t> h(sizeof(CacheState), 0);
+    CacheState *hs = reinterpret_cast<CacheState *>(h.data());
+    std::vector<float> p = initial_params(cfg->seed);
+    std::memcpy(hs->params, p.data(), sizeof(float) * kParams);
+    for (int i = 0; i < kParams; ++i) {
+        __nv_bfloat16 b = __float2bfloat16(p[i]);
+        hs->wbf[i] = b;
+    }
+    for (int a = 0; a < 3; ++a) { hs->lo[a] = cfg->scene_lo[a]; hs->hi[a] = cfg->scene_hi[a]; }
+    hs->lr = cfg->lr;
+    hs->beta1 = cfg->beta1;
+    hs->beta2 = cfg->beta2;
+    hs->eps = cfg->eps;
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(cache, h.data(), h.size(), cudaMemcpyHostToDevice, st));
+    RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_query(rt_context *ctx, rt_stream stream, const void *cache, const rt_cache_input *in,
+                                    float *out, uint32_t n) {
+    if (!ctx || !cache || (n && (!in || !out))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_query: null argument");
+    if (n == 0) return RT_OK;
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    const uint32_t tiles = (n + kQueryRows - 1) / kQueryRows;
+    uint32_t grid = (uint32_t)ctx->sm_count * 2u;
+    if (grid > tiles) grid = tiles;
+    k_cache_query<<<grid, 128, kQuerySmem, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const CacheState *>(cache), in, reinterpret_cast<float4 *>(out), n, nullptr);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_train(rt_context *ctx, rt_stream stream, void *cache, const rt_cache_input *in,
+                                    const float *targets, uint32_t n, uint32_t batch, float *loss_out) {
+    if (!ctx || !cache || (n && (!in || !targets))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_train: null argument");
+    if (batch == 0 || batch % 64u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_train: batch must be a positive multiple of 64");
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CacheState *S = static_cast<CacheState *>(cache);
+    for (uint32_t b = 0; b < n; b += batch) {
+        const uint32_t m = (n - b) < batch ? (n - b) : batch;
+        rc = launch_fwd_bwd(ctx, st, S, in + b, targets + 4u * (size_t)b, m);
+        if (rc) return rc;
+        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S);
+        k_cache_step<<<1, 32, 0, st>>>(S, loss_out);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+    }
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_gradient(rt_context *ctx, rt_stream stream, void *cache, const rt_cache_input *in,
+                                       const float *targets, uint32_t n, float *grad_out) {
+    if (!ctx || !cache || !grad_out || (n && (!in || !targets)))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_gradient: null argument");
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CacheState *S = static_cast<CacheState *>(cache);
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(S->grads, 0, sizeof(float) * kParams, st));
+    rc = launch_fwd_bwd(ctx, st, S, in, targets, n);
+    if (rc) return rc;
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(grad_out, S->grads, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(S->grads, 0, sizeof(float) * kParams, st));
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(&S->loss, 0, sizeof(float), st));
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_get_params(rt_context *ctx, rt_stream stream, const void *cache, float *params) {
+    if (!ctx || !cache || !params) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_get_params: null argument");
+    const CacheState *S = static_cast<const CacheState *>(cache);
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(params, S->params, sizeof(float) * kParams, cudaMemcpyDeviceToDevice,
+                                     static_cast<cudaStream_t>(stream)));
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_set_params(rt_context *ctx, rt_stream stream, void *cache, const float *params) {
+    if (!ctx || !cache || !params) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_set_params: null argument");
+    CacheState *S = static_cast<CacheState *>(cache);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(S->params, params, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
+    k_cache_refresh_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(S);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device-count launchers for the path tracer's learned form (no host reads,
+// no allocation): the number of query / training rows is produced on the
+// device by the shading kernels.
+// ---------------------------------------------------------------------------
+namespace rtc {
+
+int cache_query_dev(rt_context *ctx, cudaStream_t st, const void *cache, const rt_cache_input *in, float *out,
+                    const uint32_t *n_dev, uint32_t max_n) {
+    if (max_n == 0) return RT_OK;
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    const uint32_t tiles = (max_n + kQueryRows - 1) / kQueryRows;
+    uint32_t grid = (uint32_t)ctx->sm_count * 2u;
+    if (grid > tiles) grid = tiles;
+    k_cache_query<<<grid, 128, kQuerySmem, st>>>(static_cast<const CacheState *>(cache), in,
+                                                 reinterpret_cast<float4 *>(out), max_n, n_dev);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+// Adam steps over the first *n_dev samples in batches of `batch` (at most
+// max_n samples in total).
+int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cache_input *in, const float *targets,
+                    const uint32_t *n_dev, uint32_t max_n, uint32_t batch) {
+    if (max_n == 0 || batch == 0) return RT_OK;
+    int rc = set_smem(ctx);
+    if (rc) return rc;
+    CacheState *S = static_cast<CacheState *>(cache);
+    for (uint32_t b = 0; b < max_n; b += batch) {
+        const uint32_t m = (max_n - b) < batch ? (max_n - b) : batch;
+        const uint32_t tiles = (m + kTrainRows - 1) / kTrainRows;
+        uint32_t grid = (uint32_t)ctx->sm_count;
+        if (grid > tiles) grid = tiles;
+        k_cache_fwd_bwd<<<grid, 128, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(targets), m, 0.0f,
+                                                       n_dev, b);
+        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S);
+        k_cache_step<<<1, 32, 0, st>>>(S, nullptr);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+    }
+    return RT_OK;
+}
+
+}  // namespace rtc

@@ -39,10 +39,17 @@ constexpr float kRrMax = 0.95f;
 struct PtLayout {
     uint64_t rays0, rays1, pidx0, pidx1, hits, srays, spidx, scontrib, socc, tput, rad, rng, light_aux, light_cdf,
         counters, total;
-    uint32_t cap;
+    // learned form: cache queries at the second vertex and training samples
+    uint64_t qin, qout, qt1, qpidx, tin, ttarget, tt1, tlpre, tpidx;
+    uint32_t cap, train_cap;
 };
 
-PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights) {
+// counter words of the scratch counter block
+constexpr uint32_t kCntQuery = 257, kCntTrain = 258, kCntPerSample = 259;  // words [0, 259) reset per sample
+constexpr uint32_t kCntRays = 260;    // two u64
+constexpr uint32_t kCntSample = 270;  // sample index of the running wave
+
+PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap = 0) {
     PtLayout L;
     uint64_t cap = (uint64_t)p.width * p.height;
     L.cap = (uint32_t)cap;
@@ -67,11 +74,34 @@ PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights) {
     L.light_aux = take((uint64_t)(n_lights ? n_lights : 1) * 16u);
     L.light_cdf = take((uint64_t)(n_lights ? n_lights : 1) * 4u + 16u);
     // counters: [0, 65) queue lengths per vertex, [65, 129) shadow lengths,
-    // [129, 257) traversal work counters, 257 sample index, 260.. two u64 ray
-    // counts (8-byte aligned at word 260)
+    // [129, 257) traversal work counters, 257 cache queries, 258 training
+    // samples, 260.. two u64 ray counts (8-byte aligned), 270 sample index
     L.counters = take(272u * 4u);
+    L.train_cap = train_cap;
+    const uint64_t qcap = train_cap ? cap : 0;
+    L.qin = take(qcap * 48u);
+    L.qout = take(qcap * 16u);
+    L.qt1 = take(qcap * 16u);
+    L.qpidx = take(qcap * 4u);
+    L.tin = take((uint64_t)train_cap * 48u);
+    L.ttarget = take((uint64_t)train_cap * 16u);
+    L.tt1 = take((uint64_t)train_cap * 16u);
+    L.tlpre = take((uint64_t)train_cap * 16u);
+    L.tpidx = take((uint64_t)train_cap * 4u);
     L.total = off;
     return L;
+}
+
+// Training paths: pixel p of a sample is one when (p + offset) % stride == 0,
+// offset drawn per sample; exactly ceil(npix / stride) pixels qualify.
+inline uint32_t train_stride(uint64_t npix, uint32_t train_paths) {
+    if (train_paths == 0) return 0;
+    uint64_t s = npix / train_paths;
+    return (uint32_t)(s < 1 ? 1 : s);
+}
+inline uint32_t train_capacity(uint64_t npix, uint32_t train_paths) {
+    uint32_t s = train_stride(npix, train_paths);
+    return s ? (uint32_t)((npix + s - 1) / s) : 0u;
 }
 
 struct PtArgs {
@@ -101,6 +131,22 @@ struct PtArgs {
     float eps;
     unsigned long long *ray_counts;
     uint32_t *err;
+    // learned form (cache_mode != 0): at the second vertex a path either
+    // ends in a cache query or, for training pixels, records a sample and
+    // continues
+    uint32_t cache_mode;
+    uint32_t stride;          // training pixel stride
+    uint64_t seed;
+    const uint32_t *sample_dev;
+    rt_cache_input *qin;
+    float4 *qt1;
+    uint32_t *qpidx;
+    uint32_t *qcount;
+    rt_cache_input *tin;
+    float4 *tt1;
+    float4 *tlpre;
+    uint32_t *tpidx;
+    uint32_t *tcount;
 };
 
 // Per-light normal, area and the area CDF (fixed summation order).
@@ -171,6 +217,9 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = *a.count_in;
     bool want_shadow = false, want_next = false;
+    bool is_train = false, is_query = false;
+    rt_cache_input crec;
+    float4 t1 = make_float4(0.f, 0.f, 0.f, 0.f), lpre = make_float4(0.f, 0.f, 0.f, 0.f);
     float so[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, contrib[3] = {0, 0, 0};
     float no[3] = {0, 0, 0}, nd[3] = {0, 0, 0};
     uint32_t p = 0;
@@ -223,7 +272,27 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
                 if (cosd > 0.0f)
                     for (int k = 0; k < 3; ++k) nrm[k] = -nrm[k];
                 const bool reflective = m.albedo[0] > 0.0f || m.albedo[1] > 0.0f || m.albedo[2] > 0.0f;
-                if (reflective) {
+                if (reflective && a.cache_mode && a.depth == 1u) {
+                    // second vertex of the learned form: record (x, -d, n,
+                    // albedo); training pixels go on as plain path tracing,
+                    // the others end here in a cache query
+                    const uint32_t off =
+                        (uint32_t)(rtpt::splitmix64(a.seed ^ (0x5851f42d4c957f2dull + *a.sample_dev)) % a.stride);
+                    for (int k = 0; k < 3; ++k) {
+                        crec.pos[k] = P[k];
+                        crec.dir[k] = -d[k];
+                        crec.normal[k] = nrm[k];
+                        crec.albedo[k] = m.albedo[k];
+                    }
+                    t1 = T;
+                    if ((p + off) % a.stride == 0u) {
+                        is_train = true;
+                        lpre = a.rad[p];
+                    } else {
+                        is_query = true;
+                    }
+                }
+                if (reflective && !is_query) {
                     // ---- next-event estimation: one point on one light
                     if (a.n_lights > 0) {
                         const float total = a.light_cdf[a.n_lights];
@@ -305,6 +374,47 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
         a.rays_out[2u * nslot + 1u] = make_float4(nd[0], nd[1], nd[2], 1e30f);
         a.pidx_out[nslot] = p;
     }
+    if (a.cache_mode) {
+        const uint32_t tslot = warp_append(is_train, a.tcount, nullptr);
+        if (is_train) {
+            a.tin[tslot] = crec;
+            a.tt1[tslot] = t1;
+            a.tlpre[tslot] = lpre;
+            a.tpidx[tslot] = p;
+        }
+        const uint32_t qslot = warp_append(is_query, a.qcount, nullptr);
+        if (is_query) {
+            a.qin[qslot] = crec;
+            a.qt1[qslot] = t1;
+            a.qpidx[qslot] = p;
+        }
+    }
+}
+
+// Learned form, after the wave: cache-terminated paths add T1 * max(cache, 0);
+// training samples get the target (L - L_before) / T1 (the radiance their
+// plain tail brought back through the second vertex).
+__global__ void __launch_bounds__(kPtThreads) k_pt_cache_apply(const uint32_t *qcount, const uint32_t *qpidx,
+                                                                const float4 *qt1, const float4 *qout, float4 *rad,
+                                                                const uint32_t *tcount, const uint32_t *tpidx,
+                                                                const float4 *tt1, const float4 *tlpre,
+                                                                float4 *ttarget) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *qcount) {
+        const uint32_t p = qpidx[i];
+        const float4 t = qt1[i], c = qout[i];
+        float4 R = rad[p];
+        R.x = R.x + t.x * fmaxf(c.x, 0.0f);
+        R.y = R.y + t.y * fmaxf(c.y, 0.0f);
+        R.z = R.z + t.z * fmaxf(c.z, 0.0f);
+        rad[p] = R;
+    }
+    if (i < *tcount) {
+        const uint32_t p = tpidx[i];
+        const float4 t = tt1[i], l0 = tlpre[i], R = rad[p];
+        ttarget[i] = make_float4(t.x > 0.0f ? (R.x - l0.x) / t.x : 0.0f, t.y > 0.0f ? (R.y - l0.y) / t.y : 0.0f,
+                                 t.z > 0.0f ? (R.z - l0.z) / t.z : 0.0f, 0.0f);
+    }
 }
 
 __global__ void __launch_bounds__(kPtThreads) k_pt_resolve(const uint32_t *scount, const uint8_t *socc,
@@ -340,16 +450,10 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_accumulate(uint32_t n, const 
 
 using namespace rtc;
 
-extern "C" rt_status rt_pt_scratch_bytes(const rt_pt_params *p, uint64_t *bytes) {
-    if (!p || !bytes) return RT_ERR_INVALID_ARG;
-    // the light tables are sized for up to 2^20 lights by the caller's scene;
-    // the call checks again with the real count
-    *bytes = pt_layout(*p, 1u << 20).total;
-    return RT_OK;
-}
+namespace {
 
-extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
-                                   const rt_pt_params *p, float *accum, void *scratch, uint64_t scratch_bytes) {
+int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene, const rt_pt_params *p,
+                    const rt_pt_cache_params *cp, float *accum, void *scratch, uint64_t scratch_bytes) {
     if (!ctx || !scene || !p || !accum || !scratch || !scene->accel)
         return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace: null argument");
     if (!scene->tri_material || !scene->materials || scene->n_materials == 0 ||
@@ -358,11 +462,15 @@ extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_p
     if (p->max_depth == 0 || p->max_depth > kMaxPtDepth)
         return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace: max_depth must be in 1..64");
     if (scene->n_lights > (1u << 20)) return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_path_trace: more than 2^20 lights");
+    if (cp && (!cp->cache || cp->train_paths == 0 || (cp->train_batch % 64u) != 0u))
+        return set_error(ctx, RT_ERR_INVALID_ARG,
+                         "rt_path_trace_cached: cache, train_paths > 0 and a train_batch multiple of 64 are required");
     const uint64_t npix = (uint64_t)p->width * p->height;
     if (npix == 0 || p->spp == 0) return RT_OK;
     if (npix > (1u << 30)) return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_path_trace: more than 2^30 pixels");
-    const PtLayout L = pt_layout(*p, scene->n_lights);
-    if (scratch_bytes < L.total) return set_error(ctx, RT_ERR_OOM, "rt_path_trace: scratch smaller than rt_pt_scratch_bytes");
+    const uint32_t tcap = cp ? train_capacity(npix, cp->train_paths) : 0u;
+    const PtLayout L = pt_layout(*p, scene->n_lights, tcap);
+    if (scratch_bytes < L.total) return set_error(ctx, RT_ERR_OOM, "rt_path_trace: scratch smaller than the size query returned");
     if (reinterpret_cast<uintptr_t>(scratch) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace: scratch must be 256-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint8_t *S = static_cast<uint8_t *>(scratch);
@@ -370,8 +478,8 @@ extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_p
     uint32_t *cnt = reinterpret_cast<uint32_t *>(S + L.counters);
     uint32_t *scnt = cnt + 65;
     uint32_t *tcnt = cnt + 129;
-    uint32_t *sample_dev = cnt + 257;
-    unsigned long long *ray_counts = reinterpret_cast<unsigned long long *>(cnt + 260);
+    uint32_t *sample_dev = cnt + kCntSample;
+    unsigned long long *ray_counts = reinterpret_cast<unsigned long long *>(cnt + kCntRays);
     float4 *aux = reinterpret_cast<float4 *>(S + L.light_aux);
     float *cdf = reinterpret_cast<float *>(S + L.light_cdf);
 
@@ -402,13 +510,28 @@ extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_p
     a.eps = p->ray_eps;
     a.ray_counts = ray_counts;
     a.err = ctx->d_err;
+    if (cp) {
+        a.cache_mode = 1;
+        a.stride = train_stride(npix, cp->train_paths);
+        a.seed = p->seed;
+        a.sample_dev = sample_dev;
+        a.qin = reinterpret_cast<rt_cache_input *>(S + L.qin);
+        a.qt1 = reinterpret_cast<float4 *>(S + L.qt1);
+        a.qpidx = reinterpret_cast<uint32_t *>(S + L.qpidx);
+        a.qcount = cnt + kCntQuery;
+        a.tin = reinterpret_cast<rt_cache_input *>(S + L.tin);
+        a.tt1 = reinterpret_cast<float4 *>(S + L.tt1);
+        a.tlpre = reinterpret_cast<float4 *>(S + L.tlpre);
+        a.tpidx = reinterpret_cast<uint32_t *>(S + L.tpidx);
+        a.tcount = cnt + kCntTrain;
+    }
     float4 *rays[2] = {reinterpret_cast<float4 *>(S + L.rays0), reinterpret_cast<float4 *>(S + L.rays1)};
     uint32_t *pidx[2] = {reinterpret_cast<uint32_t *>(S + L.pidx0), reinterpret_cast<uint32_t *>(S + L.pidx1)};
     uint8_t *socc = S + L.socc;
     const unsigned blocks = (unsigned)((npix + kPtThreads - 1) / kPtThreads);
 
     for (uint32_t s = 0; s < p->spp; ++s) {
-        RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, 257u * 4u, st));
+        RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
         k_pt_raygen<<<blocks, kPtThreads, 0, st>>>(ax, ay, p->camera.position[0], p->camera.position[1],
                                                    p->camera.position[2], p->width, p->height, p->seed, sample_dev,
                                                    rays[0], pidx[0], a.tput, a.rad, a.rng, &cnt[0], ray_counts);
@@ -434,11 +557,56 @@ extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_p
             k_pt_resolve<<<blocks, kPtThreads, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
             RT_CUDA_CTX(ctx, cudaGetLastError());
         }
+        float4 *ttarget = reinterpret_cast<float4 *>(S + L.ttarget);
+        if (cp) {
+            int rc = cache_query_dev(ctx, st, cp->cache, a.qin, reinterpret_cast<float *>(S + L.qout), a.qcount,
+                                     (uint32_t)npix);
+            if (rc) return rc;
+            k_pt_cache_apply<<<blocks, kPtThreads, 0, st>>>(a.qcount, a.qpidx, a.qt1,
+                                                            reinterpret_cast<const float4 *>(S + L.qout), a.rad,
+                                                            a.tcount, a.tpidx, a.tt1, a.tlpre, ttarget);
+            RT_CUDA_CTX(ctx, cudaGetLastError());
+        }
         k_pt_accumulate<<<blocks, kPtThreads, 0, st>>>((uint32_t)npix, a.rad, reinterpret_cast<float4 *>(accum),
                                                        sample_dev);
         RT_CUDA_CTX(ctx, cudaGetLastError());
+        if (cp && cp->train_batch) {
+            int rc = cache_train_dev(ctx, st, cp->cache, a.tin, reinterpret_cast<const float *>(ttarget), a.tcount,
+                                     tcap, cp->train_batch);
+            if (rc) return rc;
+        }
     }
     return RT_OK;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_pt_scratch_bytes(const rt_pt_params *p, uint64_t *bytes) {
+    if (!p || !bytes) return RT_ERR_INVALID_ARG;
+    // the light tables are sized for up to 2^20 lights; the call checks the
+    // size again with the scene's real light count
+    *bytes = pt_layout(*p, 1u << 20).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_pt_cached_scratch_bytes(const rt_pt_params *p, const rt_pt_cache_params *cp,
+                                                uint64_t *bytes) {
+    if (!p || !cp || !bytes) return RT_ERR_INVALID_ARG;
+    const uint64_t npix = (uint64_t)p->width * p->height;
+    *bytes = pt_layout(*p, 1u << 20, train_capacity(npix, cp->train_paths)).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
+                                   const rt_pt_params *p, float *accum, void *scratch, uint64_t scratch_bytes) {
+    return path_trace_impl(ctx, stream, scene, p, nullptr, accum, scratch, scratch_bytes);
+}
+
+extern "C" rt_status rt_path_trace_cached(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
+                                          const rt_pt_params *p, const rt_pt_cache_params *cp, float *accum,
+                                          void *scratch, uint64_t scratch_bytes) {
+    if (!cp) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace_cached: null cache parameters");
+    return path_trace_impl(ctx, stream, scene, p, cp, accum, scratch, scratch_bytes);
 }
 
 extern "C" rt_status rt_pt_ray_counts(rt_context *ctx, rt_stream stream, const rt_pt_params *p, uint32_t n_lights,
@@ -448,7 +616,7 @@ extern "C" rt_status rt_pt_ray_counts(rt_context *ctx, rt_stream stream, const r
     unsigned long long h[2];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint8_t *S = static_cast<const uint8_t *>(scratch);
-    RT_CUDA_CTX(ctx, cudaMemcpyAsync(h, S + L.counters + 260u * 4u, sizeof(h), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(h, S + L.counters + kCntRays * 4u, sizeof(h), cudaMemcpyDeviceToHost, st));
     RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
     if (extension_rays) *extension_rays = h[0];
     if (shadow_rays) *shadow_rays = h[1];

@@ -117,6 +117,20 @@ class PtParams(C.Structure):
                 ("seed", C.c_uint64), ("ray_eps", C.c_float), ("flags", C.c_uint32)]
 
 
+class CacheConfig(C.Structure):
+    _fields_ = [("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("seed", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+def cache_config(lo=(-1.0, -1.0, -1.0), hi=(1.0, 1.0, 1.0), lr=1e-3, beta1=0.9, beta2=0.99, eps=1e-8,
+                 seed=1) -> CacheConfig:
+    return CacheConfig((C.c_float * 3)(*lo), (C.c_float * 3)(*hi), lr, beta1, beta2, eps, seed, 0)
+
+
+class PtCacheParams(C.Structure):
+    _fields_ = [("cache", C.c_void_p), ("train_paths", C.c_uint32), ("train_batch", C.c_uint32)]
+
+
 assert C.sizeof(PtLight) == 48
 assert C.sizeof(GeometryTriangles) == 48
 assert C.sizeof(Instance) == 64
@@ -155,6 +169,18 @@ PROTOTYPES = {
     "rt_pt_scratch_bytes": (_i32, [C.POINTER(PtParams), C.POINTER(_u64)]),
     "rt_path_trace": (_i32, [_vp, _vp, C.POINTER(PtScene), C.POINTER(PtParams), _vp, _vp, _u64]),
     "rt_pt_ray_counts": (_i32, [_vp, _vp, C.POINTER(PtParams), _u32, _vp, C.POINTER(_u64), C.POINTER(_u64)]),
+    "rt_pt_cached_scratch_bytes": (_i32, [C.POINTER(PtParams), C.POINTER(PtCacheParams), C.POINTER(_u64)]),
+    "rt_path_trace_cached": (_i32, [_vp, _vp, C.POINTER(PtScene), C.POINTER(PtParams), C.POINTER(PtCacheParams), _vp,
+                                    _vp, _u64]),
+    # MLP radiance cache declared in include/rtcore_cache.h
+    "rt_cache_bytes": (_i32, [C.POINTER(_u64)]),
+    "rt_cache_param_count": (_u32, []),
+    "rt_cache_init": (_i32, [_vp, _vp, _vp, _vp]),
+    "rt_cache_query": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32]),
+    "rt_cache_train": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp]),
+    "rt_cache_gradient": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32, _vp]),
+    "rt_cache_get_params": (_i32, [_vp, _vp, _vp, _vp]),
+    "rt_cache_set_params": (_i32, [_vp, _vp, _vp, _vp]),
     # seeded scenes declared in include/rtcore_scene.h (host code)
     "rt_scene_soup": (_i32, [_u64, _u32, _vp, _vp]),
     "rt_scene_box_counts": (_i32, [_u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
@@ -321,11 +347,52 @@ class Context:
         self.check(self.lib.rt_path_trace(self.h, _stream_ptr(stream), C.byref(scene), C.byref(params), _ptr(accum),
                                           _ptr(scratch), scratch_bytes), "rt_path_trace")
 
+    def pt_cached_scratch_bytes(self, params: PtParams, cp: PtCacheParams) -> int:
+        out = C.c_uint64()
+        self.check(self.lib.rt_pt_cached_scratch_bytes(C.byref(params), C.byref(cp), C.byref(out)),
+                   "rt_pt_cached_scratch_bytes")
+        return out.value
+
+    def path_trace_cached(self, scene: PtScene, params: PtParams, cp: PtCacheParams, accum, scratch,
+                          scratch_bytes: int, stream=None) -> None:
+        self.check(self.lib.rt_path_trace_cached(self.h, _stream_ptr(stream), C.byref(scene), C.byref(params),
+                                                 C.byref(cp), _ptr(accum), _ptr(scratch), scratch_bytes),
+                   "rt_path_trace_cached")
+
     def pt_ray_counts(self, params: PtParams, n_lights: int, scratch, stream=None):
         e, s = C.c_uint64(), C.c_uint64()
         self.check(self.lib.rt_pt_ray_counts(self.h, _stream_ptr(stream), C.byref(params), n_lights, _ptr(scratch),
                                              C.byref(e), C.byref(s)), "rt_pt_ray_counts")
         return e.value, s.value
+
+    # ---- MLP radiance cache
+    def cache_bytes(self) -> int:
+        out = C.c_uint64()
+        self.check(self.lib.rt_cache_bytes(C.byref(out)), "rt_cache_bytes")
+        return out.value
+
+    def cache_init(self, cache, cfg: "CacheConfig", stream=None) -> None:
+        self.check(self.lib.rt_cache_init(self.h, _stream_ptr(stream), _ptr(cache), C.byref(cfg)), "rt_cache_init")
+
+    def cache_query(self, cache, inputs, out, n: int, stream=None) -> None:
+        self.check(self.lib.rt_cache_query(self.h, _stream_ptr(stream), _ptr(cache), _ptr(inputs), _ptr(out), n),
+                   "rt_cache_query")
+
+    def cache_train(self, cache, inputs, targets, n: int, batch: int, loss_out=None, stream=None) -> None:
+        self.check(self.lib.rt_cache_train(self.h, _stream_ptr(stream), _ptr(cache), _ptr(inputs), _ptr(targets), n,
+                                           batch, _ptr(loss_out)), "rt_cache_train")
+
+    def cache_gradient(self, cache, inputs, targets, n: int, grad_out, stream=None) -> None:
+        self.check(self.lib.rt_cache_gradient(self.h, _stream_ptr(stream), _ptr(cache), _ptr(inputs), _ptr(targets),
+                                              n, _ptr(grad_out)), "rt_cache_gradient")
+
+    def cache_get_params(self, cache, params, stream=None) -> None:
+        self.check(self.lib.rt_cache_get_params(self.h, _stream_ptr(stream), _ptr(cache), _ptr(params)),
+                   "rt_cache_get_params")
+
+    def cache_set_params(self, cache, params, stream=None) -> None:
+        self.check(self.lib.rt_cache_set_params(self.h, _stream_ptr(stream), _ptr(cache), _ptr(params)),
+                   "rt_cache_set_params")
 
     # ---- utilities
     def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:

@@ -1,0 +1,169 @@
+"""Equal-time relMSE of the learned form (MLP radiance cache) against the plain
+path tracer, both measured against a converged plain reference.
+
+    python -m rtcore.relmse [--spheres 160 --freq 50] [--width 1920 --height 1080]
+                            [--ref-spp 16384] [--budget-ms 4000] [--out result.json]
+
+relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Both
+forms run one sample per call; the time of a call is its CUDA-event duration
+(training included for the learned form), image read-backs are not timed.
+The curve is sampled at doubling sample counts and at the end of the budget.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import Camera, Context, GeometryTriangles, PtCacheParams, PtParams, PtScene, cache_config, load
+from . import scenes as S
+
+
+def relmse(img: np.ndarray, ref: np.ndarray) -> float:
+    return float(np.mean((img - ref) ** 2 / (ref * ref + 0.01)))
+
+
+class GpuBox:
+    """The box workload on the device: BLAS, materials, lights."""
+
+    def __init__(self, ctx: Context, n_spheres: int, freq: int, seed: int = S.SEED_BASE + 3):
+        import torch
+        self.ctx = ctx
+        v, i, tm, m = S.box(seed, n_spheres, freq)
+        self.n_tris = len(i)
+        lights = S.emissive_lights(v, i, tm, m)
+        self.keep = [torch.from_numpy(v.reshape(-1)).cuda(), torch.from_numpy(i.reshape(-1).view(np.int32)).cuda(),
+                     torch.from_numpy(tm.view(np.int32)).cuda(), torch.from_numpy(m.view(np.uint8)).cuda(),
+                     torch.from_numpy(lights.view(np.uint8)).cuda()]
+        g = GeometryTriangles()
+        g.vertices, g.vertex_stride, g.max_vertex = self.keep[0].data_ptr(), 12, len(v) - 1
+        g.index_type, g.indices, g.tri_count, g.flags = 1, self.keep[1].data_ptr(), len(i), 1
+        sz = ctx.blas_sizes([len(i)])
+        self.accel = torch.empty(sz.accel_bytes, dtype=torch.uint8, device="cuda")
+        scratch = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device="cuda")
+        ctx.build_blas([g], 0, self.accel, sz.accel_bytes, scratch, sz.scratch_bytes)
+        ctx.sync()
+        del scratch
+        self.n_lights = len(lights)
+        self.scene = PtScene(ctx.address(self.accel), self.keep[2].data_ptr(), self.keep[3].data_ptr(), len(m),
+                             self.keep[4].data_ptr(), len(lights))
+
+
+def params(w: int, h: int, spp: int, offset: int, seed: int) -> PtParams:
+    return PtParams(Camera(S.BOX_CAMERA[0], S.BOX_CAMERA[1]), w, h, spp, offset, 8, 3, seed, 1e-4, 0)
+
+
+def _image(accum) -> np.ndarray:
+    a = accum.cpu().numpy().view(np.float32).reshape(-1, 4)
+    return a[:, :3] / np.maximum(a[:, 3:4], 1.0)
+
+
+def reference(ctx: Context, box: GpuBox, w: int, h: int, spp: int, chunk: int = 256, seed: int = 12345) -> np.ndarray:
+    import torch
+    p = params(w, h, min(chunk, spp), 0, seed)
+    nb = ctx.pt_scratch_bytes(p)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    accum = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
+    done = 0
+    while done < spp:
+        p = params(w, h, min(chunk, spp - done), done, seed)
+        ctx.path_trace(box.scene, p, accum, scratch, nb)
+        done += p.spp
+    ctx.sync()
+    return _image(accum)
+
+
+def _checkpoints(n: int):
+    k = 1
+    while k <= n:
+        yield k
+        k *= 2
+
+
+def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, cached: bool,
+        train_paths: int = 65536, train_batch: int = 16384, seed: int = 777, lr: float = 1e-3):
+    """[(elapsed_ms, samples, relmse)] within the time budget."""
+    import torch
+    st = torch.cuda.current_stream()
+    accum = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
+    p = params(w, h, 1, 0, seed)
+    cache = None
+    if cached:
+        cache = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device="cuda")
+        ctx.cache_init(cache, cache_config(lr=lr, seed=3))
+        cp = PtCacheParams(cache.data_ptr(), train_paths, train_batch)
+        nb = ctx.pt_cached_scratch_bytes(p, cp)
+    else:
+        nb = ctx.pt_scratch_bytes(p)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    curve, elapsed, s = [], 0.0, 0
+    marks = set(_checkpoints(1 << 20))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    while elapsed < budget_ms:
+        p = params(w, h, 1, s, seed)
+        e0.record(st)
+        if cached:
+            ctx.path_trace_cached(box.scene, p, cp, accum, scratch, nb)
+        else:
+            ctx.path_trace(box.scene, p, accum, scratch, nb)
+        e1.record(st)
+        e1.synchronize()
+        elapsed += e0.elapsed_time(e1)
+        s += 1
+        if s in marks or elapsed >= budget_ms:
+            curve.append((round(elapsed, 3), s, relmse(_image(accum), ref)))
+    ctx.sync()
+    return curve
+
+
+def time_to(curve, target: float):
+    """First elapsed time at which relMSE <= target (None if never)."""
+    for ms, s, r in curve:
+        if r <= target:
+            return ms
+    return None
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--spheres", type=int, default=160)
+    ap.add_argument("--freq", type=int, default=50)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--ref-spp", type=int, default=16384)
+    ap.add_argument("--budget-ms", type=float, default=4000.0)
+    ap.add_argument("--target", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--train-paths", type=int, default=65536, help="training paths per frame")
+    ap.add_argument("--train-batch", type=int, default=16384)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    load()
+    ctx = Context(0)
+    t0 = time.time()
+    box = GpuBox(ctx, a.spheres, a.freq)
+    ref = reference(ctx, box, a.width, a.height, a.ref_spp)
+    t_ref = time.time() - t0
+    plain = run(ctx, box, a.width, a.height, ref, a.budget_ms, False)
+    cached = run(ctx, box, a.width, a.height, ref, a.budget_ms, True, train_paths=a.train_paths,
+                 train_batch=a.train_batch, lr=a.lr)
+    res = {"tris": box.n_tris, "width": a.width, "height": a.height, "ref_spp": a.ref_spp,
+           "train_paths": a.train_paths, "train_batch": a.train_batch, "lr": a.lr,
+           "reference_wall_s": round(t_ref, 1), "budget_ms": a.budget_ms,
+           "plain": plain, "cached": cached,
+           "relmse_at_budget": {"plain": plain[-1][2], "cached": cached[-1][2]},
+           "time_to_target_ms": {"target": a.target, "plain": time_to(plain, a.target),
+                                 "cached": time_to(cached, a.target)}}
+    js = json.dumps(res)
+    print(js)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(js + "\n")
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

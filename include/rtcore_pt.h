@@ -64,6 +64,30 @@ rt_status rt_pt_scratch_bytes(const rt_pt_params *p, uint64_t *bytes);
 rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene, const rt_pt_params *p,
                         float *accum, void *scratch, uint64_t scratch_bytes);
 
+/*
+ * Learned form: the MLP radiance cache of rtcore_cache.h ends paths at their
+ * second vertex.  Per sample, about train_paths pixels (an exact residue
+ * class of the pixel index, re-drawn every sample) are training paths: they
+ * continue as plain path tracing, and the radiance their tail brings back
+ * through the second vertex (divided by the throughput there) is a training
+ * target for (position, direction toward the first vertex, normal, albedo).
+ * Every other path adds throughput x max(cache, 0) at its second vertex and
+ * stops.  After the wave the cache takes ceil(train_paths / train_batch) Adam
+ * steps on the new samples (train_batch 0: no training).  The cache's
+ * emission is not included: direct light reaches the first vertex through
+ * next-event estimation only, as in the plain form.
+ */
+typedef struct rt_pt_cache_params {
+    void *cache;            /* rt_cache state (device)            */
+    uint32_t train_paths;   /* training paths per sample, > 0     */
+    uint32_t train_batch;   /* Adam batch, multiple of 64, or 0   */
+} rt_pt_cache_params;
+
+rt_status rt_pt_cached_scratch_bytes(const rt_pt_params *p, const rt_pt_cache_params *cp, uint64_t *bytes);
+
+rt_status rt_path_trace_cached(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene, const rt_pt_params *p,
+                               const rt_pt_cache_params *cp, float *accum, void *scratch, uint64_t scratch_bytes);
+
 /* Extension rays (camera + bounce) and shadow rays traced by the last
  * rt_path_trace call that used `scratch` with these parameters and light
  * count (synchronises `stream`). */
