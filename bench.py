@@ -371,6 +371,8 @@ def run_ours(args) -> int:
     e2e_ms = e0.elapsed_time(e1) / k_e2e
     e2e_value = n_all * world / (e2e_ms * 1e-3) / 1e6
 
+    extra = secondary_workloads(ctx, stream, dev) if (rank == 0 and not args.no_secondary) else {}
+
     out = None
     if rank == 0:
         cpu = None
@@ -397,12 +399,105 @@ def run_ours(args) -> int:
                              "shadow_anyhit_mrays": round(shadow_mrays, 2),
                              "build_ms": round(statistics.median(build_ms), 3),
                              "wall_s_timed_region": round(t_wall, 3)},
+               "secondary": extra,
                "clocks": clocks.summary()}
         print(json.dumps(out), flush=True)
     ctx.close()
     if dist:
         tdist.destroy_process_group()
     return 0
+
+
+def _events(torch, stream, fn, reps: int) -> float:
+    """Mean milliseconds of fn() over reps calls, CUDA events on `stream`."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def secondary_workloads(ctx, stream, dev) -> dict:
+    """Untimed-by-the-headline figures of the other targets: the 2M-triangle
+    box scene (build, primary and incoherent rays), the path tracer on it at
+    1920x1080, and the MLP cache's query and training throughput."""
+    import torch
+    import rtcore
+    import rtcore.scenes as S
+    out = {}
+    v, i, tm, m = S.box(S.SEED_BASE + 3, 40, 50)
+    lights = S.emissive_lights(v, i, tm, m)
+    keep = [torch.from_numpy(v.reshape(-1)).to(dev), torch.from_numpy(i.reshape(-1).view(np.int32)).to(dev),
+            torch.from_numpy(tm.view(np.int32)).to(dev), torch.from_numpy(m.view(np.uint8)).to(dev),
+            torch.from_numpy(lights.view(np.uint8)).to(dev)]
+    g = rtcore.GeometryTriangles()
+    g.vertices, g.vertex_stride, g.max_vertex = keep[0].data_ptr(), 12, len(v) - 1
+    g.index_type, g.indices, g.tri_count, g.flags = rtcore.RT_INDEX_UINT32, keep[1].data_ptr(), len(i), 1
+    sz = ctx.blas_sizes([len(i)])
+    accel = torch.empty(sz.accel_bytes, dtype=torch.uint8, device=dev)
+    scratch = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device=dev)
+    build = lambda: ctx.build_blas([g], 0, accel, sz.accel_bytes, scratch, sz.scratch_bytes, stream)
+    build()
+    ms_build = _events(torch, stream, build, 5)
+    ctx.sync(stream)
+    del scratch
+    addr = ctx.address(accel)
+    n = W * H
+    rays = torch.empty(n * 32, dtype=torch.uint8, device=dev)
+    ctx.generate_primary_rays(rtcore.Camera(S.BOX_CAMERA[0], S.BOX_CAMERA[1]), W, H, 0.0, 1e30, rays, stream)
+    inc = torch.from_numpy(S.incoherent_rays(S.SEED_BASE + 3, n, (-0.99,) * 3, (0.99,) * 3, 1e30).view(np.uint8)).to(dev)
+    hits = torch.empty(n * 16, dtype=torch.uint8, device=dev)
+    for r in (rays, inc):
+        ctx.trace_closest(addr, r, hits, n, stream=stream)
+    ms_p = _events(torch, stream, lambda: ctx.trace_closest(addr, rays, hits, n, stream=stream), 20)
+    ms_i = _events(torch, stream, lambda: ctx.trace_closest(addr, inc, hits, n, stream=stream), 20)
+    out["box_2M"] = {"tris": len(i), "build_ms": round(ms_build, 3), "primary_mrays": round(n / ms_p / 1e3, 1),
+                     "incoherent_mrays": round(n / ms_i / 1e3, 1),
+                     "targets": "north_star: >= 2000 primary, >= 500 incoherent Mrays/s on the 2M-triangle scene"}
+    # path tracer, 1920x1080, 4 samples per call, depth 8, RR from 3
+    sc = rtcore.PtScene(addr, keep[2].data_ptr(), keep[3].data_ptr(), len(m), keep[4].data_ptr(), len(lights))
+    p = rtcore.PtParams(rtcore.Camera(S.BOX_CAMERA[0], S.BOX_CAMERA[1]), W, H, 4, 0, 8, 3, S.SEED_BASE + 3, 1e-4, 0)
+    nb = ctx.pt_scratch_bytes(p)
+    pscr = torch.empty(nb, dtype=torch.uint8, device=dev)
+    acc = torch.zeros(n * 16, dtype=torch.uint8, device=dev)
+    ctx.path_trace(sc, p, acc, pscr, nb, stream)
+    ms_pt = _events(torch, stream, lambda: ctx.path_trace(sc, p, acc, pscr, nb, stream), 3)
+    ext, shadow = ctx.pt_ray_counts(p, len(lights), pscr, stream)
+    out["path_tracer"] = {"resolution": [W, H], "spp_per_call": 4, "ms_per_spp": round(ms_pt / 4, 3),
+                          "mrays_per_s": round((ext + shadow) / ms_pt / 1e3, 1),
+                          "rays_per_spp": round((ext + shadow) / 4 / n, 3)}
+    del pscr, acc
+    # MLP cache: 2M queries (43,520 FLOP each, algorithmic) and 65,536 training
+    # samples per pass (120,192 FLOP each)
+    cache = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device=dev)
+    ctx.cache_init(cache, rtcore.cache_config(seed=1), stream)
+    rng = np.random.default_rng(0)
+    qn = n
+    qin = np.zeros((qn, 12), np.float32)
+    qin[:, 0:3] = rng.uniform(-1, 1, (qn, 3))
+    for c0 in (3, 6):
+        d = rng.normal(size=(qn, 3))
+        qin[:, c0:c0 + 3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    qin[:, 9:12] = rng.uniform(0, 1, (qn, 3))
+    dq = torch.from_numpy(qin.reshape(-1)).to(dev)
+    qo = torch.empty(qn * 16, dtype=torch.uint8, device=dev)
+    ctx.cache_query(cache, dq, qo, qn, stream)
+    ms_q = _events(torch, stream, lambda: ctx.cache_query(cache, dq, qo, qn, stream), 10)
+    tn = 65536
+    tg = torch.from_numpy(rng.uniform(0, 1, (tn, 4)).astype(np.float32).reshape(-1)).to(dev)
+    ctx.cache_train(cache, dq, tg, tn, 16384, None, stream)
+    ms_t = _events(torch, stream, lambda: ctx.cache_train(cache, dq, tg, tn, 16384, None, stream), 5)
+    peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text()) if (REPO / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    q_tflops = qn * 43520 / (ms_q * 1e-3) / 1e12
+    out["mlp_cache"] = {"query_ms_2M": round(ms_q, 3), "query_tflops": round(q_tflops, 2),
+                        "query_frac_of_bf16_peak": round(q_tflops / bf16_peak, 4),
+                        "train_ms_65536": round(ms_t, 3),
+                        "train_tflops": round(tn * 120192 / (ms_t * 1e-3) / 1e12, 2)}
+    ctx.sync(stream)
+    return out
 
 
 def main(argv=None) -> int:
@@ -414,6 +509,7 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the box-scene / path-tracer / MLP figures")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
