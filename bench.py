@@ -51,6 +51,9 @@ WORKLOAD = "triangle soup 1M tris (unit cube, edges U(0.001,0.02)); 1920x1080 pr
 BYTES_RAY_IO = 48   # 32 B ray in + 16 B hit out
 BYTES_NODE = 80     # compressed BVH8 node
 BYTES_TRI = 36      # FP32 vertex triplet
+# DRAM bytes (read + write) of one step's two traversal launches measured by
+# ncu (cold caches): 97.5 MB primary + 392.0 MB incoherent
+TRAFFIC_BYTES_PER_STEP = 489_500_000
 
 
 def _env_int(name: str, default: int) -> int:
@@ -317,7 +320,12 @@ def run_ours(args) -> int:
     alg_bytes = n_p * bytes_p + n_i * bytes_i
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "frac": round(achieved / peaks["hbm_gbs"], 4),
+                # dram__bytes_read.sum + dram__bytes_write.sum of the two
+                # launches of one step, from one ncu capture of this workload
+                # (cold caches): profiles/k_trace_blas_soup1M_1920x1080.md
+                "traffic": TRAFFIC_BYTES_PER_STEP,
+                "algorithmic_bytes_per_step": round(alg_bytes),
                 "peak_source": peaks["source"],
                 "kernel": "k_trace_blas (closest hit)",
                 "bytes_per_ray": {"primary": round(bytes_p, 1), "incoherent": round(bytes_i, 1)},

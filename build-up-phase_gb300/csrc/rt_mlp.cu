@@ -7,11 +7,13 @@
 //   layer 0: 96 (81 used) -> 64, ReLU
 //   layers 1-4: 64 -> 64, ReLU
 //   layer 5: 64 -> 8 (3 used), linear
-// Forward: one warp owns 16 rows; each layer is m16n8k16 BF16 MMAs with FP32
-// accumulation; the FP32 accumulator fragment of one layer is exactly the
-// A-operand fragment layout of the next (after bias, ReLU and BF16 packing),
-// so activations never leave registers between layers.  Weights sit in
-// shared memory with padded row strides (bank-conflict free fragment loads).
+// Inference (queries): tcgen05 MMAs with TMEM accumulators, see
+// k_cache_query_tc.
+// Training forward: one warp owns 16 rows; each layer is m16n8k16 BF16 MMAs
+// with FP32 accumulation; the FP32 accumulator fragment of one layer is
+// exactly the A-operand fragment layout of the next (after bias, ReLU and
+// BF16 packing), so activations never leave registers between layers.
+// Weights sit in shared memory with padded row strides.
 // Backward (training): the same MMA routine propagates delta through W^T
 // (transposed into shared memory at block start); weight gradients are FP32
 // outer products on the CUDA cores over the 64-row tile, added to global
@@ -144,14 +146,18 @@ __device__ void encode_row(const rt_cache_input &in, const CacheState *S, __nv_b
     for (int a = 0; a < 3; ++a) {
         const float ext = S->hi[a] - S->lo[a];
         const float pn = ext > 0.0f ? (in.pos[a] - S->lo[a]) / ext : 0.0f;
-        float scale = 1.0f;
+        // octave k = sin/cos(2^k pi x): one sincospif, then the double-angle
+        // recurrence (the error doubles per octave: ~2^11 ulp after 11
+        // octaves, far below the BF16 rounding of the features)
+        float s, c;
+        sincospif(pn, &s, &c);
 #pragma unroll
         for (int k = 0; k < 12; ++k) {
-            float s, c;
-            sincospif(scale * pn, &s, &c);
             f[24 * a + 2 * k] = s;
             f[24 * a + 2 * k + 1] = c;
-            scale *= 2.0f;
+            const float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
+            s = s2;
+            c = c2;
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -188,61 +194,7 @@ __device__ void load_weights(const CacheState *S, __nv_bfloat16 *sW, __nv_bfloat
         for (int e = threadIdx.x; e < out_dim(l); e += blockDim.x) sB[(l < 5 ? 64 * l : 320) + e] = S->params[b_off(l) + e];
 }
 
-// ---------------------------------------------------------------------------
-// Inference: 128 rows per tile, 4 warps x 2 slabs of 16 rows
-// ---------------------------------------------------------------------------
-
 constexpr int kQueryRows = 128;
-constexpr size_t kQuerySmem = (size_t)kSwElems * 2 + (size_t)kBiasFloats * 4 + (size_t)kQueryRows * kInStride * 2;
-
-__global__ void __launch_bounds__(128) k_cache_query(const CacheState *S, const rt_cache_input *in, float4 *out,
-                                                     uint32_t n, const uint32_t *n_dev) {
-    if (n_dev) n = min(n, *n_dev);  // row count produced on the device
-    extern __shared__ __align__(16) uint8_t smem[];
-    __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smem);
-    float *sB = reinterpret_cast<float *>(sW + kSwElems);
-    __nv_bfloat16 *sIn = reinterpret_cast<__nv_bfloat16 *>(sB + kBiasFloats);
-    load_weights(S, sW, nullptr, sB);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, q = lane & 3;
-    const uint32_t tiles = (n + kQueryRows - 1) / kQueryRows;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        __syncthreads();  // weights loaded / previous tile done with sIn
-        const uint32_t row = tile * kQueryRows + threadIdx.x;
-        if (row < n) {
-            encode_row(in[row], S, sIn + threadIdx.x * kInStride);
-        } else {
-            for (int k = 0; k < 96; k += 2) *reinterpret_cast<uint32_t *>(sIn + threadIdx.x * kInStride + k) = 0u;
-        }
-        __syncthreads();
-#pragma unroll 1
-        for (int slab = 0; slab < 2; ++slab) {
-            const int r0 = warp * 32 + slab * 16;
-            uint32_t a0[6][4];
-            load_a<6>(sIn, kInStride, r0, lane, a0);
-            float c[8][4];
-            warp_dense<6, 8>(a0, sW + sw_off(0), w_stride(0), sB, c, lane);
-            uint32_t a[4][4];
-            relu_to_a(c, a);
-#pragma unroll 1
-            for (int l = 1; l <= 4; ++l) {
-                warp_dense<4, 8>(a, sW + sw_off(l), w_stride(l), sB + 64 * l, c, lane);
-                relu_to_a(c, a);
-            }
-            float y[1][4];
-            warp_dense<4, 1>(a, sW + sw_off(5), w_stride(5), sB + 320, y, lane);
-            // y[0]: rows g / g+8, cols 2q, 2q+1 -> gather the 3 outputs of a row
-            // into one float4 store by lanes q == 0 (cols 0,1) and q == 1 (col 2)
-            const float c2_g = __shfl_sync(0xffffffffu, y[0][0], (lane & ~3) | 1);
-            const float c2_g8 = __shfl_sync(0xffffffffu, y[0][2], (lane & ~3) | 1);
-            if (q == 0) {
-                const uint32_t ra = tile * kQueryRows + r0 + g, rb = ra + 8;
-                if (ra < n) out[ra] = make_float4(y[0][0], y[0][1], c2_g, 0.0f);
-                if (rb < n) out[rb] = make_float4(y[0][2], y[0][3], c2_g8, 0.0f);
-            }
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Training: forward + backward over 64-row tiles, gradients into S->grads
@@ -417,6 +369,231 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
     if (lane == 0) atomicAdd(&S->loss, loss * inv_count);
 }
 
+// ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05 + TMEM)
+// ---------------------------------------------------------------------------
+//
+// One CTA = 4 warps = 128 threads, one query row per thread, 128-row tiles.
+// Operands live in shared memory in the canonical K-major layout without
+// swizzle: 8-row x 16-byte core matrices; element (r, k) of a tile with K
+// columns sits at (r/8)*16K + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes, so one
+// MMA step of K = 16 is described by LBO = 128 (next core matrix along K) and
+// SBO = 16K (next 8-row group).  Thread 0 issues tcgen05.mma.kind::f16 with
+// M = 128, N = 64 (N = 16 for the output layer), K = 16 per instruction,
+// BF16 x BF16 -> FP32 accumulators in TMEM (row r = TMEM lane r), and commits
+// to an mbarrier.  The epilogue of every thread reads its row's 64
+// accumulators with tcgen05.ld (each warp its own 32-lane quarter), adds the
+// bias, applies ReLU, packs BF16 and writes the row into the next layer's
+// A tile; fence.proxy.async makes those generic-proxy stores visible to the
+// next MMA.  Every mbarrier wait is bounded: on expiry the kernel records
+// RT_ERR_TIMEOUT, waits once more (bounded) for its MMAs, frees its TMEM and
+// returns.
+
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcTmemCols = 128;
+// tile byte sizes / offsets
+__host__ __device__ constexpr uint32_t tc_tile_bytes(int rows, int k) { return (uint32_t)(rows / 8) * 16u * k; }
+__host__ __device__ constexpr uint32_t tc_w_off(int l) {
+    uint32_t o = 0;
+    for (int i = 0; i < l; ++i) o += tc_tile_bytes(i == 5 ? 16 : 64, in_dim(i));
+    return o;
+}
+constexpr uint32_t kTcWBytes = tc_w_off(6);                       // 47104
+constexpr uint32_t kTcA0 = kTcWBytes;                             // input tile, K = 96
+constexpr uint32_t kTcH0 = kTcA0 + tc_tile_bytes(kTcRows, 96);    // hidden tiles, K = 64
+constexpr uint32_t kTcH1 = kTcH0 + tc_tile_bytes(kTcRows, 64);
+constexpr uint32_t kTcBias = kTcH1 + tc_tile_bytes(kTcRows, 64);  // 336 floats
+constexpr uint32_t kTcBar = kTcBias + 336u * 4u;                  // mbarrier (8 B) + TMEM address (4 B)
+constexpr uint32_t kTcSmem = kTcBar + 64u;
+constexpr int kTcSpinLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint32_t tc_off(int r, int k, int kdim) {
+    return (uint32_t)(r >> 3) * 16u * (uint32_t)kdim + (uint32_t)(k >> 3) * 128u + (uint32_t)(r & 7) * 16u +
+           (uint32_t)(k & 7) * 2u;
+}
+// Shared-memory matrix descriptor: start >> 4, LBO >> 4, SBO >> 4,
+// descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::f16: FP32 accumulate (bits 4-5 = 1), BF16
+// A and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < kTcSpinLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__global__ void __launch_bounds__(128, 2) k_cache_query_tc(const CacheState *S, const rt_cache_input *in, float4 *out,
+                                                            uint32_t n, const uint32_t *n_dev, uint32_t *err) {
+    if (n_dev) n = min(n, *n_dev);
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint8_t *sW = smem;
+    float *sB = reinterpret_cast<float *>(smem + kTcBias);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kTcBar);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcBar + 8);
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // ---- weights (canonical K-major) and biases into shared memory
+    for (int l = 0; l < kLayers; ++l) {
+        const int kin = in_dim(l), nout = l == 5 ? 16 : 64, nreal = out_dim(l);
+        const __nv_bfloat16 *gw = S->wbf + w_off(l);
+        __nv_bfloat16 *dst = reinterpret_cast<__nv_bfloat16 *>(sW + tc_w_off(l));
+        for (int e = tid; e < nout * kin; e += 128) {
+            const int o = e / kin, i = e % kin;
+            dst[tc_off(o, i, kin) / 2] = o < nreal ? gw[o * kin + i] : __float2bfloat16(0.0f);
+        }
+    }
+    for (int e = tid; e < 336; e += 128) {
+        const int l = e < 320 ? e / 64 : 5, o = e < 320 ? e % 64 : e - 320;
+        sB[e] = o < out_dim(l) ? S->params[b_off(l) + o] : 0.0f;
+    }
+    if (tid == 0) {
+        s_fail = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+        // make the initialised barrier visible to the tensor core's arrivals
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t bar_a = smem_u32(bar);
+    const uint32_t w_base = smem_u32(sW);
+    uint32_t phase = 0;
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !s_fail; tile += gridDim.x) {
+        // ---- encode this thread's row into the K = 96 input tile
+        const uint32_t row = tile * kTcRows + (uint32_t)tid;
+        {
+            __align__(16) __nv_bfloat16 feat[96];
+            if (row < n) {
+                encode_row(in[row], S, feat);
+            } else {
+                for (int k = 0; k < 96; ++k) feat[k] = __float2bfloat16(0.0f);
+            }
+            for (int kc = 0; kc < 12; ++kc)
+                *reinterpret_cast<uint4 *>(smem + kTcA0 + tc_off(tid, 8 * kc, 96)) =
+                    *reinterpret_cast<const uint4 *>(feat + 8 * kc);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+#pragma unroll 1
+        for (int l = 0; l < kLayers; ++l) {
+            const int kin = in_dim(l);
+            const uint32_t a_base = smem_u32(smem + (l == 0 ? kTcA0 : ((l & 1) ? kTcH0 : kTcH1)));
+            const uint32_t b_base = w_base + tc_w_off(l);
+            if (tid == 0) {
+                const uint32_t idesc = tc_idesc(kTcRows, l == 5 ? 16 : 64);
+                for (int ks = 0; ks < kin / 16; ++ks) {
+                    const uint64_t da = tc_desc(a_base + 256u * ks, 128u, 16u * kin);
+                    const uint64_t db = tc_desc(b_base + 256u * ks, 128u, 16u * kin);
+                    tc_mma(tmem, da, db, idesc, ks > 0 ? 1u : 0u);
+                }
+                tc_commit(bar_a);
+            }
+            const bool ok = mbar_wait_bounded(bar_a, phase);
+            phase ^= 1u;
+            if (!ok) {
+                report_error(err, RT_ERR_TIMEOUT, 0x90000000u | (uint32_t)l);
+                atomicExch(&s_fail, 1);
+            }
+            tc_fence_after();
+            if (l < 5) {
+                // hidden layer: bias + ReLU -> BF16 row of the next A tile
+                uint8_t *next = smem + ((l & 1) ? kTcH1 : kTcH0);
+                const float *bias = sB + 64 * l;
+#pragma unroll
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    float v[16];
+                    tc_ld16(tmem + lane_base + 16u * c16, v);
+                    tc_wait_ld();
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        packed[k] = pack_bf16(fmaxf(v[2 * k] + bias[16 * c16 + 2 * k], 0.0f),
+                                              fmaxf(v[2 * k + 1] + bias[16 * c16 + 2 * k + 1], 0.0f));
+                    *reinterpret_cast<uint4 *>(next + tc_off(tid, 16 * c16, 64)) =
+                        make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    *reinterpret_cast<uint4 *>(next + tc_off(tid, 16 * c16 + 8, 64)) =
+                        make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            } else {
+                float v[16];
+                tc_ld16(tmem + lane_base, v);
+                tc_wait_ld();
+                if (row < n) out[row] = make_float4(v[0] + sB[320], v[1] + sB[321], v[2] + sB[322], 0.0f);
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (s_fail) break;
+        }
+    }
+    // ---- teardown: no MMA may still be running when TMEM is freed
+    __syncthreads();
+    if (s_fail && tid == 0) mbar_wait_bounded(bar_a, phase);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+}
+
 __global__ void k_cache_adam(CacheState *S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
@@ -448,7 +625,7 @@ __global__ void k_cache_refresh_bf16(CacheState *S) {
 }
 
 int set_smem(rt_context *ctx) {
-    RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_query, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQuerySmem));
+    RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_query_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
     RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
     return RT_OK;
 }
@@ -536,8 +713,8 @@ extern "C" rt_status rt_cache_query(rt_context *ctx, rt_stream stream, const voi
     const uint32_t tiles = (n + kQueryRows - 1) / kQueryRows;
     uint32_t grid = (uint32_t)ctx->sm_count * 2u;
     if (grid > tiles) grid = tiles;
-    k_cache_query<<<grid, 128, kQuerySmem, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const CacheState *>(cache), in, reinterpret_cast<float4 *>(out), n, nullptr);
+    k_cache_query_tc<<<grid, 128, kTcSmem, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const CacheState *>(cache), in, reinterpret_cast<float4 *>(out), n, nullptr, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }
@@ -611,8 +788,8 @@ int cache_query_dev(rt_context *ctx, cudaStream_t st, const void *cache, const r
     const uint32_t tiles = (max_n + kQueryRows - 1) / kQueryRows;
     uint32_t grid = (uint32_t)ctx->sm_count * 2u;
     if (grid > tiles) grid = tiles;
-    k_cache_query<<<grid, 128, kQuerySmem, st>>>(static_cast<const CacheState *>(cache), in,
-                                                 reinterpret_cast<float4 *>(out), max_n, n_dev);
+    k_cache_query_tc<<<grid, 128, kTcSmem, st>>>(static_cast<const CacheState *>(cache), in,
+                                                 reinterpret_cast<float4 *>(out), max_n, n_dev, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }

@@ -67,6 +67,22 @@ def test_forward_matches_oracle(ctx, cache):
     assert np.all(y[:, 3] == 0)
 
 
+def test_forward_many_tiles_matches_oracle(ctx, cache):
+    """100,003 rows: several 128-row tiles per CTA and a ragged last tile."""
+    from oracle import mlp
+    import torch
+    x = random_inputs(100003, 11)
+    out = torch.full((len(x) * 4,), -7.0, dtype=torch.float32, device="cuda")
+    ctx.cache_query(cache, dev(x), out, len(x))
+    ctx.sync()
+    y = out.cpu().numpy().reshape(-1, 4)
+    assert np.isfinite(y).all() and not (y[:, 0] == -7.0).any()
+    idx = np.r_[np.random.default_rng(0).choice(len(x) - 64, 2000, replace=False), np.arange(len(x) - 64, len(x))]
+    p = get_params(ctx, cache)
+    yo = mlp.forward(p, x[idx], (-1, -1, -1), (1, 1, 1))[:, :3]
+    assert np.abs(y[idx, :3] - yo).max() / np.abs(yo).max() < 1e-2
+
+
 def test_gradient_matches_oracle(ctx, cache):
     from oracle import mlp
     import torch
