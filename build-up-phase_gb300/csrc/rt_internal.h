@@ -57,6 +57,25 @@ inline void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *
 int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
                        uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any);
 
+// Launch shape of the multi-scene traversal (rt_trace_multi.cu).
+struct TraceShape {
+    uint32_t threads;        // 128 or 256
+    uint32_t blocks_per_sm;
+    uint32_t ring;           // 8, 16 or 32 shared-memory stack entries per ray
+    uint32_t refill;         // 1..32
+};
+
+// Queue-driven traversal over rays of many scenes: ray i belongs to scene
+// ray_scene[i], whose 32-byte traversal view is views[ray_scene[i]]
+// (TravScene of rt_traverse.cuh).  Closest hits carry the leaf-record index.
+int launch_queue_trace_multi(rt_context *ctx, cudaStream_t st, const void *views, uint32_t n_scenes,
+                             const uint32_t *ray_scene, const void *rays, void *hits, uint8_t *occluded,
+                             const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any,
+                             const TraceShape &shape);
+
+// Loads the two traversal kernels of a shape (before a graph capture).
+int prepare_queue_trace_multi(rt_context *ctx, const TraceShape &shape);
+
 // MLP cache launchers whose row counts live on the device (rt_mlp.cu).
 int cache_query_dev(rt_context *ctx, cudaStream_t st, const void *cache, const rt_cache_input *in, float *out,
                     const uint32_t *n_dev, uint32_t max_n);

@@ -23,10 +23,16 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
 
+#include "../../include/rtcore_batch.h"
 #include "../../include/rtcore_pt.h"
 #include "rt_internal.h"
 #include "rt_pt_math.cuh"
+#include "rt_traverse.cuh"
 
 namespace rtc {
 namespace {
@@ -104,6 +110,24 @@ inline uint32_t train_capacity(uint64_t npix, uint32_t train_paths) {
     return s ? (uint32_t)((npix + s - 1) / s) : 0u;
 }
 
+// One scene of a batch on the device (96 bytes).  Paths of a sample pass are
+// numbered across the scenes: scene s owns global paths [base, base + w*h).
+struct BtScene {
+    const uint8_t *accel;
+    const uint32_t *tri_material;
+    const rt_material *materials;
+    const rt_pt_light *lights;
+    float4 *accum;
+    uint32_t n_materials, n_lights;
+    uint32_t light_off;  // first entry of the scene's light tables (its CDF starts at light_off + scene)
+    uint32_t width, height;
+    uint32_t base;
+    float ax, ay;
+    float cam[3];
+    uint32_t pad[3];
+};
+static_assert(sizeof(BtScene) == 96, "BtScene layout");
+
 struct PtArgs {
     const uint8_t *accel;      // bottom-level structure (leaf records behind its header)
     const uint32_t *tri_material;
@@ -147,12 +171,17 @@ struct PtArgs {
     float4 *tlpre;
     uint32_t *tpidx;
     uint32_t *tcount;
+    // batch (multi-scene kernels): each queue entry carries its scene
+    const BtScene *bt;
+    uint32_t wave_base;        // global path index of slot 0 of the wave
+    const uint32_t *rsid_in;
+    uint32_t *rsid_out;
+    uint32_t *ssid;
 };
 
-// Per-light normal, area and the area CDF (fixed summation order).
-__global__ void k_pt_setup(const rt_pt_light *lights, uint32_t n_lights, float4 *aux, float *cdf, uint32_t *sample_dev,
-                           uint32_t sample_offset, unsigned long long *ray_counts) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+// Per-light normal, area and the area CDF (fixed summation order), one
+// thread per scene.
+__device__ void light_table(const rt_pt_light *lights, uint32_t n_lights, float4 *aux, float *cdf) {
     float acc = 0.0f;
     for (uint32_t k = 0; k < n_lights; ++k) {
         const rt_pt_light &l = lights[k];
@@ -168,6 +197,12 @@ __global__ void k_pt_setup(const rt_pt_light *lights, uint32_t n_lights, float4 
         cdf[k] = acc;
     }
     cdf[n_lights] = acc;
+}
+
+__global__ void k_pt_setup(const rt_pt_light *lights, uint32_t n_lights, float4 *aux, float *cdf, uint32_t *sample_dev,
+                           uint32_t sample_offset, unsigned long long *ray_counts) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    light_table(lights, n_lights, aux, cdf);
     *sample_dev = sample_offset;
     ray_counts[0] = 0ull;
     ray_counts[1] = 0ull;
@@ -213,21 +248,45 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *count, unsi
     return want ? base + (uint32_t)__popc(mask & ((1u << lane) - 1u)) : 0xffffffffu;
 }
 
-__global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = *a.count_in;
+// Shades queue entry i (all 32 lanes of the warp call it together: the
+// queue appends are warp-wide).  MULTI: the entry's scene comes from the
+// queue and the scene table; otherwise from the arguments.
+template <bool MULTI>
+__device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t n) {
     bool want_shadow = false, want_next = false;
     bool is_train = false, is_query = false;
     rt_cache_input crec;
     float4 t1 = make_float4(0.f, 0.f, 0.f, 0.f), lpre = make_float4(0.f, 0.f, 0.f, 0.f);
     float so[3] = {0, 0, 0}, sd[3] = {0, 0, 0}, contrib[3] = {0, 0, 0};
     float no[3] = {0, 0, 0}, nd[3] = {0, 0, 0};
-    uint32_t p = 0;
+    uint32_t p = 0, sid = 0;
     if (i < n) {
         p = a.pidx_in[i];
+        const uint8_t *accel = a.accel;
+        const uint32_t *tri_material = a.tri_material;
+        const rt_material *materials = a.materials;
+        uint32_t n_materials = a.n_materials;
+        const rt_pt_light *lights = a.lights;
+        const float4 *light_aux = a.light_aux;
+        const float *light_cdf = a.light_cdf;
+        uint32_t n_lights = a.n_lights;
+        uint32_t pix = p;  // pixel index within the scene: the random stream
+        if (MULTI) {
+            sid = a.rsid_in[i];
+            const BtScene &sc = a.bt[sid];
+            accel = sc.accel;
+            tri_material = sc.tri_material;
+            materials = sc.materials;
+            n_materials = sc.n_materials;
+            lights = sc.lights;
+            light_aux = a.light_aux + sc.light_off;
+            light_cdf = a.light_cdf + sc.light_off + sid;
+            n_lights = sc.n_lights;
+            pix = a.wave_base + p - sc.base;
+        }
         rtpt::Pcg g;
         g.state = a.rng[p];
-        g.inc = ((uint64_t)p << 1u) | 1u;
+        g.inc = ((uint64_t)pix << 1u) | 1u;
         float u[6];
         for (int k = 0; k < 6; ++k) u[k] = rtpt::pcg_uniform(g);
         a.rng[p] = g.state;
@@ -236,8 +295,8 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
         if (rec != 0xffffffffu) {
             const float4 r0 = a.rays_in[2u * i], r1 = a.rays_in[2u * i + 1u];
             const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
-            const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
-            const uint4 *pr = reinterpret_cast<const uint4 *>(a.accel + hd->prim_offset) + (size_t)rec * 3u;
+            const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(accel);
+            const uint4 *pr = reinterpret_cast<const uint4 *>(accel + hd->prim_offset) + (size_t)rec * 3u;
             const uint4 q0 = __ldg(pr), q1 = __ldg(pr + 1), q2 = __ldg(pr + 2);
             const float v0[3] = {__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z)};
             const float v1[3] = {__uint_as_float(q1.x), __uint_as_float(q1.y), __uint_as_float(q1.z)};
@@ -255,12 +314,12 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
             if (len > 0.0f) {
                 for (int k = 0; k < 3; ++k) nrm[k] = ng[k] / len;
                 const float cosd = rtpt::dot3(nrm, d);
-                uint32_t mi = a.tri_material[tri];
-                if (mi >= a.n_materials) {
+                uint32_t mi = tri_material[tri];
+                if (mi >= n_materials) {
                     report_error(a.err, RT_ERR_BOUNDS, 0x80000000u | tri);
                     mi = 0;
                 }
-                const rt_material m = a.materials[mi];
+                const rt_material m = materials[mi];
                 float4 T = a.tput[p];
                 if (a.depth == 0 && cosd < 0.0f) {
                     float4 R = a.rad[p];
@@ -272,7 +331,7 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
                 if (cosd > 0.0f)
                     for (int k = 0; k < 3; ++k) nrm[k] = -nrm[k];
                 const bool reflective = m.albedo[0] > 0.0f || m.albedo[1] > 0.0f || m.albedo[2] > 0.0f;
-                if (reflective && a.cache_mode && a.depth == 1u) {
+                if (!MULTI && reflective && a.cache_mode && a.depth == 1u) {
                     // second vertex of the learned form: record (x, -d, n,
                     // albedo); training pixels go on as plain path tracing,
                     // the others end here in a cache query
@@ -294,16 +353,16 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
                 }
                 if (reflective && !is_query) {
                     // ---- next-event estimation: one point on one light
-                    if (a.n_lights > 0) {
-                        const float total = a.light_cdf[a.n_lights];
+                    if (n_lights > 0) {
+                        const float total = light_cdf[n_lights];
                         const float target = u[0] * total;
-                        uint32_t lo = 0, hi = a.n_lights - 1u;
+                        uint32_t lo = 0, hi = n_lights - 1u;
                         while (lo < hi) {  // first k with cdf[k] > target
                             uint32_t mid = (lo + hi) >> 1;
-                            if (a.light_cdf[mid] > target) hi = mid; else lo = mid + 1u;
+                            if (light_cdf[mid] > target) hi = mid; else lo = mid + 1u;
                         }
-                        const rt_pt_light L = a.lights[lo];
-                        const float4 ln = a.light_aux[lo];
+                        const rt_pt_light L = lights[lo];
+                        const float4 ln = light_aux[lo];
                         const float su = sqrtf(u[1]);
                         const float b0 = 1.0f - su, b1 = u[2] * su;
                         const float b2 = (1.0f - b0) - b1;
@@ -367,14 +426,16 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
         a.srays[2u * sslot + 1u] = make_float4(sd[0], sd[1], sd[2], kShadowTmax);
         a.spidx[sslot] = p;
         a.scontrib[sslot] = make_float4(contrib[0], contrib[1], contrib[2], 0.0f);
+        if (MULTI) a.ssid[sslot] = sid;
     }
     const uint32_t nslot = warp_append(want_next, a.count_out, a.ray_counts);
     if (want_next) {
         a.rays_out[2u * nslot] = make_float4(no[0], no[1], no[2], 0.0f);
         a.rays_out[2u * nslot + 1u] = make_float4(nd[0], nd[1], nd[2], 1e30f);
         a.pidx_out[nslot] = p;
+        if (MULTI) a.rsid_out[nslot] = sid;
     }
-    if (a.cache_mode) {
+    if (!MULTI && a.cache_mode) {
         const uint32_t tslot = warp_append(is_train, a.tcount, nullptr);
         if (is_train) {
             a.tin[tslot] = crec;
@@ -389,6 +450,16 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_shade(const PtArgs a) {
             a.qpidx[qslot] = p;
         }
     }
+}
+
+// Grid-stride over the queue (a grid of resident blocks, not one thread
+// per pixel: deep bounces leave short queues).
+template <bool MULTI>
+__global__ void __launch_bounds__(512) k_pt_shade(const PtArgs a) {
+    const uint32_t n = *a.count_in;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t w = blockIdx.x * blockDim.x + (threadIdx.x - lane); w < n; w += gridDim.x * blockDim.x)
+        shade_one<MULTI>(a, w + lane, n);
 }
 
 // Learned form, after the wave: cache-terminated paths add T1 * max(cache, 0);
@@ -417,18 +488,19 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_cache_apply(const uint32_t *q
     }
 }
 
-__global__ void __launch_bounds__(kPtThreads) k_pt_resolve(const uint32_t *scount, const uint8_t *socc,
-                                                            const uint32_t *spidx, const float4 *scontrib,
-                                                            float4 *rad) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *scount || socc[i]) return;
-    const uint32_t p = spidx[i];
-    const float4 c = scontrib[i];
-    float4 R = rad[p];
-    R.x = R.x + c.x;
-    R.y = R.y + c.y;
-    R.z = R.z + c.z;
-    rad[p] = R;
+__global__ void __launch_bounds__(512) k_pt_resolve(const uint32_t *scount, const uint8_t *socc,
+                                                     const uint32_t *spidx, const float4 *scontrib, float4 *rad) {
+    const uint32_t n = *scount;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (socc[i]) continue;
+        const uint32_t p = spidx[i];
+        const float4 c = scontrib[i];
+        float4 R = rad[p];
+        R.x = R.x + c.x;
+        R.y = R.y + c.y;
+        R.z = R.z + c.z;
+        rad[p] = R;
+    }
 }
 
 __global__ void __launch_bounds__(kPtThreads) k_pt_accumulate(uint32_t n, const float4 *rad, float4 *accum,
@@ -445,12 +517,133 @@ __global__ void __launch_bounds__(kPtThreads) k_pt_accumulate(uint32_t n, const 
     accum[p] = acc;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batch: many scenes per launch (rtcore_batch.h).  The paths of one sample
+// pass are numbered across the scenes; a wave holds up to `cap` consecutive
+// paths, and every queue entry carries the index of its scene.
+// ---------------------------------------------------------------------------
+
+// Per launch: each scene's traversal view and light tables; ray counters.
+__global__ void k_bt_setup(const BtScene *bt, uint32_t n_scenes, TravScene *views, float4 *aux, float *cdf,
+                           unsigned long long *ray_counts, uint32_t *err) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) {
+        ray_counts[0] = 0ull;
+        ray_counts[1] = 0ull;
+    }
+    if (s >= n_scenes) return;
+    const BtScene &sc = bt[s];
+    TravScene v;
+    v.nodes = nullptr;
+    v.prims = nullptr;
+    v.node_count = 0u;
+    v.prim_count = 0u;
+    v.pad[0] = v.pad[1] = 0u;
+    const bool used = sc.width != 0u && sc.height != 0u;  // no path refers to a scene without pixels
+    if (used && sc.accel) {
+        const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(sc.accel);
+        if (hd->kind == RT_ACCEL_KIND_BLAS) {
+            v.nodes = reinterpret_cast<const uint4 *>(sc.accel + hd->node_offset);
+            v.prims = reinterpret_cast<const uint4 *>(sc.accel + hd->prim_offset);
+            v.node_count = hd->prim_count ? hd->node_count : 0u;
+            v.prim_count = hd->prim_count;
+        } else {
+            // the path tracer shades bottom-level structures only
+            report_error(err, RT_ERR_UNSUPPORTED, 0x78000000u | s);
+        }
+    }
+    views[s] = v;
+    if (used) light_table(sc.lights, sc.n_lights, aux + sc.light_off, cdf + sc.light_off + s);
+}
+
+__global__ void __launch_bounds__(512) k_bt_raygen(const BtScene *bt, uint32_t n_scenes, uint32_t wave_base,
+                                                   uint32_t n, uint64_t seed, const uint32_t *sample_dev,
+                                                   uint32_t pass, float4 *rays, uint32_t *pidx, uint32_t *rsid,
+                                                   uint32_t *psid, float4 *tput, float4 *rad, uint64_t *rng,
+                                                   uint32_t *count0, unsigned long long *ray_counts) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) {
+        *count0 = n;
+        atomicAdd(ray_counts, (unsigned long long)n);
+    }
+    if (p >= n) return;
+    const uint32_t gp = wave_base + p;
+    // the last scene whose first path is <= gp (a scene without pixels shares
+    // its base with the next one)
+    uint32_t lo = 0, hi = n_scenes - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (bt[mid].base <= gp) lo = mid; else hi = mid - 1u;
+    }
+    const BtScene &sc = bt[lo];
+    const uint32_t pix = gp - sc.base;
+    const uint32_t x = pix % sc.width, y = pix / sc.width;
+    rtpt::Pcg g = rtpt::pcg_seed(seed, *sample_dev + pass, pix);
+    const float jx = rtpt::pcg_uniform(g), jy = rtpt::pcg_uniform(g);
+    float d[3];
+    rtpt::camera_dir(sc.ax, sc.ay, sc.width, sc.height, x, y, jx, jy, d);
+    rays[2u * p] = make_float4(sc.cam[0], sc.cam[1], sc.cam[2], 0.0f);
+    rays[2u * p + 1u] = make_float4(d[0], d[1], d[2], 1e30f);
+    pidx[p] = p;
+    rsid[p] = lo;
+    psid[p] = lo;
+    tput[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    rad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    rng[p] = g.state;
+}
+
+__global__ void __launch_bounds__(512) k_bt_accumulate(const BtScene *bt, uint32_t wave_base, uint32_t n,
+                                                       const uint32_t *psid, const float4 *rad, uint32_t discard) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n || discard) return;
+    const BtScene &sc = bt[psid[p]];
+    float4 *acc = sc.accum + (wave_base + p - sc.base);
+    const float4 r = rad[p];
+    float4 v = *acc;
+    v.x = v.x + r.x;
+    v.y = v.y + r.y;
+    v.z = v.z + r.z;
+    v.w = v.w + 1.0f;
+    *acc = v;
+}
+
+__global__ void k_bt_sample(uint32_t *sample_dev, uint32_t value, uint32_t add) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *sample_dev = add ? *sample_dev + value : value;
+}
+
 }  // namespace
 }  // namespace rtc
 
 using namespace rtc;
 
 namespace {
+
+// Blocks of `threads` resident on the GPU at once for `kernel`, capped by the
+// blocks n items need (grid-stride kernels).
+unsigned resident_blocks(rt_context *ctx, const void *kernel, int threads, uint64_t n) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find({kernel, threads});
+        if (it != cache.end()) {
+            per_sm = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+                per_sm < 1) {
+                (void)cudaGetLastError();
+                per_sm = 1;
+            }
+            cache[{kernel, threads}] = per_sm;
+        }
+    }
+    const uint64_t need = (n + (uint64_t)threads - 1u) / (uint64_t)threads;
+    const uint64_t have = (uint64_t)per_sm * (uint64_t)ctx->sm_count;
+    const uint64_t b = need < have ? need : have;
+    return (unsigned)(b ? b : 1u);
+}
 
 int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene, const rt_pt_params *p,
                     const rt_pt_cache_params *cp, float *accum, void *scratch, uint64_t scratch_bytes) {
@@ -529,6 +722,8 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
     uint32_t *pidx[2] = {reinterpret_cast<uint32_t *>(S + L.pidx0), reinterpret_cast<uint32_t *>(S + L.pidx1)};
     uint8_t *socc = S + L.socc;
     const unsigned blocks = (unsigned)((npix + kPtThreads - 1) / kPtThreads);
+    const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<false>, kPtThreads, npix);
+    const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, kPtThreads, npix);
 
     for (uint32_t s = 0; s < p->spp; ++s) {
         RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
@@ -549,12 +744,12 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
             a.count_out = &cnt[d + 1];
             a.scount = &scnt[d];
             a.depth = d;
-            k_pt_shade<<<blocks, kPtThreads, 0, st>>>(a);
+            k_pt_shade<false><<<shade_blocks, kPtThreads, 0, st>>>(a);
             RT_CUDA_CTX(ctx, cudaGetLastError());
             rc = launch_queue_trace(ctx, st, accel, a.srays, nullptr, socc, &scnt[d], (uint32_t)npix,
                                     &tcnt[2 * d + 1], true);
             if (rc) return rc;
-            k_pt_resolve<<<blocks, kPtThreads, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
+            k_pt_resolve<<<resolve_blocks, kPtThreads, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
             RT_CUDA_CTX(ctx, cudaGetLastError());
         }
         float4 *ttarget = reinterpret_cast<float4 *>(S + L.ttarget);
@@ -620,5 +815,427 @@ extern "C" rt_status rt_pt_ray_counts(rt_context *ctx, rt_stream stream, const r
     RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
     if (extension_rays) *extension_rays = h[0];
     if (shadow_rays) *shadow_rays = h[1];
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batch host side (rtcore_batch.h)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct BtLayout {
+    uint64_t table, views, light_aux, light_cdf, counters;
+    uint64_t rays0, rays1, pidx0, pidx1, rsid0, rsid1, hits, srays, spidx, ssid, scontrib, socc, tput, rad, rng, psid;
+    uint64_t total;
+    uint64_t cap;  // paths per wave
+};
+
+BtLayout bt_layout(uint32_t n_scenes, uint64_t n_lights, uint64_t cap) {
+    BtLayout L;
+    L.cap = cap;
+    uint64_t off = 0;
+    auto take = [&](uint64_t b) {
+        uint64_t o = off;
+        off += align_up(b ? b : 1, 256);
+        return o;
+    };
+    L.table = take((uint64_t)n_scenes * sizeof(BtScene));
+    L.views = take((uint64_t)n_scenes * sizeof(TravScene));
+    L.light_aux = take(n_lights * 16u);
+    L.light_cdf = take((n_lights + n_scenes) * 4u);
+    L.counters = take(272u * 4u);  // word layout of the single-scene path tracer
+    L.rays0 = take(cap * 32u);
+    L.rays1 = take(cap * 32u);
+    L.pidx0 = take(cap * 4u);
+    L.pidx1 = take(cap * 4u);
+    L.rsid0 = take(cap * 4u);
+    L.rsid1 = take(cap * 4u);
+    L.hits = take(cap * 16u);
+    L.srays = take(cap * 32u);
+    L.spidx = take(cap * 4u);
+    L.ssid = take(cap * 4u);
+    L.scontrib = take(cap * 16u);
+    L.socc = take(cap);
+    L.tput = take(cap * 16u);
+    L.rad = take(cap * 16u);
+    L.rng = take(cap * 8u);
+    L.psid = take(cap * 4u);
+    L.total = off;
+    return L;
+}
+
+constexpr uint64_t kMaxBatchPaths = (1ull << 31) - 1u;  // paths of one sample pass over all scenes
+constexpr uint64_t kMaxBatchLights = 1ull << 26;
+
+// Totals of a scene table; RT_OK or an error message in *why.
+int batch_totals(const rt_batch_scene *scenes, uint32_t n, uint64_t *paths, uint64_t *lights, const char **why) {
+    uint64_t P = 0, NL = 0;
+    for (uint32_t s = 0; s < n; ++s) {
+        const rt_batch_scene &b = scenes[s];
+        const uint64_t npix = (uint64_t)b.width * b.height;
+        if (npix) {
+            if (!b.scene.accel || !b.accum || !b.scene.tri_material || !b.scene.materials ||
+                b.scene.n_materials == 0 || (b.scene.n_lights && !b.scene.lights)) {
+                *why = "rt_batch: a scene with pixels needs accel, accum, tri_material and materials (and lights)";
+                return RT_ERR_INVALID_ARG;
+            }
+            if (b.scene.n_lights > (1u << 20)) {
+                *why = "rt_batch: more than 2^20 lights in a scene";
+                return RT_ERR_UNSUPPORTED;
+            }
+        }
+        P += npix;
+        NL += b.scene.n_lights;
+    }
+    if (P > kMaxBatchPaths || NL > kMaxBatchLights) {
+        *why = "rt_batch: more than 2^31 - 1 pixels or 2^26 lights in one batch";
+        return RT_ERR_UNSUPPORTED;
+    }
+    *paths = P;
+    *lights = NL;
+    return RT_OK;
+}
+
+// Zero fields take the defaults; RT_OK or RT_ERR_INVALID_ARG.
+int batch_tuning(const rt_batch_tuning *in, rt_batch_tuning *out) {
+    rt_batch_tuning t;
+    rt_batch_default_tuning(&t);
+    if (in) {
+        if (in->trace_threads) t.trace_threads = in->trace_threads;
+        if (in->trace_blocks_per_sm) t.trace_blocks_per_sm = in->trace_blocks_per_sm;
+        if (in->stack_ring) t.stack_ring = in->stack_ring;
+        if (in->refill) t.refill = in->refill;
+        if (in->shade_threads) t.shade_threads = in->shade_threads;
+        t.wave_paths = in->wave_paths;
+        if (in->bvh_width) t.bvh_width = in->bvh_width;
+    }
+    if ((t.trace_threads != 128u && t.trace_threads != 256u) ||
+        (t.stack_ring != 8u && t.stack_ring != 16u && t.stack_ring != 32u) || t.refill > 32u ||
+        t.trace_blocks_per_sm > 64u || (t.shade_threads != 128u && t.shade_threads != 256u && t.shade_threads != 512u) ||
+        t.bvh_width != 8u)
+        return RT_ERR_INVALID_ARG;
+    *out = t;
+    return RT_OK;
+}
+
+}  // namespace
+
+struct rt_batch_plan {
+    rt_context *ctx = nullptr;
+    uint32_t n_scenes = 0;
+    rt_batch_params p{};
+    rt_batch_tuning t{};
+    uint32_t flags = 0;
+    BtLayout L{};
+    uint8_t *scratch = nullptr;
+    uint64_t paths = 0;       // per sample pass
+    uint32_t kernels = 0;     // kernel launches per rt_batch_launch
+    cudaGraphExec_t exec = nullptr;
+    bool sample_known = false;
+    uint32_t next_sample = 0;
+};
+
+namespace {
+
+int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
+    rt_context *ctx = pl->ctx;
+    const BtLayout &L = pl->L;
+    uint8_t *S = pl->scratch;
+    uint32_t k = 0;
+    *kernels = 0;
+    if (pl->paths == 0) return RT_OK;
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(S + L.counters);
+    uint32_t *scnt = cnt + 65;
+    uint32_t *tcnt = cnt + 129;
+    uint32_t *sample_dev = cnt + kCntSample;
+    unsigned long long *ray_counts = reinterpret_cast<unsigned long long *>(cnt + kCntRays);
+    const BtScene *bt = reinterpret_cast<const BtScene *>(S + L.table);
+    void *views = S + L.views;
+    float4 *aux = reinterpret_cast<float4 *>(S + L.light_aux);
+    float *cdf = reinterpret_cast<float *>(S + L.light_cdf);
+    const unsigned T = pl->t.shade_threads;
+    const uint32_t n_sc = pl->n_scenes;
+
+    k_bt_setup<<<(n_sc + 127u) / 128u, 128, 0, st>>>(bt, n_sc, reinterpret_cast<TravScene *>(views), aux, cdf,
+                                                      ray_counts, ctx->d_err);
+    ++k;
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+
+    PtArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.light_aux = aux;
+    a.light_cdf = cdf;
+    a.tput = reinterpret_cast<float4 *>(S + L.tput);
+    a.rad = reinterpret_cast<float4 *>(S + L.rad);
+    a.rng = reinterpret_cast<uint64_t *>(S + L.rng);
+    a.hits = reinterpret_cast<const float4 *>(S + L.hits);
+    a.srays = reinterpret_cast<float4 *>(S + L.srays);
+    a.spidx = reinterpret_cast<uint32_t *>(S + L.spidx);
+    a.ssid = reinterpret_cast<uint32_t *>(S + L.ssid);
+    a.scontrib = reinterpret_cast<float4 *>(S + L.scontrib);
+    a.max_depth = pl->p.max_depth;
+    a.rr_depth = pl->p.rr_depth;
+    a.eps = pl->p.ray_eps;
+    a.ray_counts = ray_counts;
+    a.err = ctx->d_err;
+    a.bt = bt;
+    float4 *rays[2] = {reinterpret_cast<float4 *>(S + L.rays0), reinterpret_cast<float4 *>(S + L.rays1)};
+    uint32_t *pidx[2] = {reinterpret_cast<uint32_t *>(S + L.pidx0), reinterpret_cast<uint32_t *>(S + L.pidx1)};
+    uint32_t *rsid[2] = {reinterpret_cast<uint32_t *>(S + L.rsid0), reinterpret_cast<uint32_t *>(S + L.rsid1)};
+    uint32_t *psid = reinterpret_cast<uint32_t *>(S + L.psid);
+    uint8_t *socc = S + L.socc;
+    const TraceShape shape{pl->t.trace_threads, pl->t.trace_blocks_per_sm, pl->t.stack_ring, pl->t.refill};
+    const uint64_t W = L.cap;
+    const uint64_t waves = (pl->paths + W - 1u) / W;
+    const uint32_t discard = (pl->flags & RT_BATCH_DISCARD) ? 1u : 0u;
+
+    for (uint32_t pass = 0; pass < pl->p.spp; ++pass) {
+        for (uint64_t w = 0; w < waves; ++w) {
+            const uint32_t base = (uint32_t)(w * W);
+            const uint32_t n = (uint32_t)(pl->paths - base < W ? pl->paths - base : W);
+            const unsigned full = (n + T - 1u) / T;
+            const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<true>, (int)T, n);
+            const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, (int)T, n);
+            RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
+            k_bt_raygen<<<full, T, 0, st>>>(bt, n_sc, base, n, pl->p.seed, sample_dev, pass, rays[0], pidx[0],
+                                            rsid[0], psid, a.tput, a.rad, a.rng, &cnt[0], ray_counts);
+            ++k;
+            RT_CUDA_CTX(ctx, cudaGetLastError());
+            a.wave_base = base;
+            for (uint32_t d = 0; d < pl->p.max_depth; ++d) {
+                const uint32_t q = d & 1u;
+                int rc = launch_queue_trace_multi(ctx, st, views, n_sc, rsid[q], rays[q], S + L.hits, nullptr, &cnt[d],
+                                                  n, &tcnt[2 * d], false, shape);
+                if (rc) return rc;
+                ++k;
+                a.rays_in = rays[q];
+                a.pidx_in = pidx[q];
+                a.rsid_in = rsid[q];
+                a.rays_out = rays[q ^ 1u];
+                a.pidx_out = pidx[q ^ 1u];
+                a.rsid_out = rsid[q ^ 1u];
+                a.count_in = &cnt[d];
+                a.count_out = &cnt[d + 1];
+                a.scount = &scnt[d];
+                a.depth = d;
+                k_pt_shade<true><<<shade_blocks, T, 0, st>>>(a);
+                ++k;
+                RT_CUDA_CTX(ctx, cudaGetLastError());
+                rc = launch_queue_trace_multi(ctx, st, views, n_sc, a.ssid, a.srays, nullptr, socc, &scnt[d], n,
+                                              &tcnt[2 * d + 1], true, shape);
+                if (rc) return rc;
+                ++k;
+                k_pt_resolve<<<resolve_blocks, T, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
+                ++k;
+                RT_CUDA_CTX(ctx, cudaGetLastError());
+            }
+            k_bt_accumulate<<<full, T, 0, st>>>(bt, base, n, psid, a.rad, discard);
+            ++k;
+            RT_CUDA_CTX(ctx, cudaGetLastError());
+        }
+    }
+    k_bt_sample<<<1, 32, 0, st>>>(sample_dev, pl->p.spp, 1u);
+    ++k;
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    *kernels = k;
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_batch_default_tuning(rt_batch_tuning *t) {
+    if (!t) return RT_ERR_INVALID_ARG;
+    t->trace_threads = 128u;
+    t->trace_blocks_per_sm = 8u;
+    t->stack_ring = 16u;
+    t->refill = 4u;
+    t->shade_threads = 256u;
+    t->wave_paths = 0u;
+    t->bvh_width = 8u;
+    t->reserved = 0u;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_scratch_bytes(const rt_batch_scene *scenes, uint32_t n_scenes, const rt_batch_params *p,
+                                            const rt_batch_tuning *t, uint64_t *bytes) {
+    if (!bytes || !p || (n_scenes && !scenes)) return RT_ERR_INVALID_ARG;
+    uint64_t P = 0, NL = 0;
+    const char *why = nullptr;
+    int rc = batch_totals(scenes, n_scenes, &P, &NL, &why);
+    if (rc) return rc;
+    rt_batch_tuning tt;
+    if (batch_tuning(t, &tt)) return RT_ERR_INVALID_ARG;
+    const uint64_t cap = (tt.wave_paths && tt.wave_paths < P) ? tt.wave_paths : P;
+    *bytes = bt_layout(n_scenes, NL, cap).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene *scenes, uint32_t n_scenes,
+                                          const rt_batch_params *p, const rt_batch_tuning *t, void *scratch,
+                                          uint64_t scratch_bytes, uint32_t flags, rt_batch_plan **plan) {
+    if (!ctx || !p || !plan || (n_scenes && !scenes) || !scratch)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: null argument");
+    *plan = nullptr;
+    if (flags & ~(RT_BATCH_GRAPH | RT_BATCH_DISCARD))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: unknown flags");
+    if (p->max_depth == 0 || p->max_depth > kMaxPtDepth || p->spp == 0 || p->flags || p->reserved)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: spp >= 1, max_depth in 1..64, flags 0");
+    uint64_t P = 0, NL = 0;
+    const char *why = nullptr;
+    int rc = batch_totals(scenes, n_scenes, &P, &NL, &why);
+    if (rc) return set_error(ctx, rc, why);
+    rt_batch_tuning tt;
+    if (batch_tuning(t, &tt))
+        return set_error(ctx, RT_ERR_INVALID_ARG,
+                         "rt_batch_plan_create: tuning needs 128/256 trace threads, ring 8/16/32, refill <= 32, "
+                         "128/256/512 shade threads, BVH width 8");
+    const uint64_t cap = (tt.wave_paths && tt.wave_paths < P) ? tt.wave_paths : P;
+    const BtLayout L = bt_layout(n_scenes, NL, cap);
+    if (scratch_bytes < L.total)
+        return set_error(ctx, RT_ERR_OOM, "rt_batch_plan_create: scratch smaller than rt_batch_scratch_bytes");
+    if (reinterpret_cast<uintptr_t>(scratch) & 255u)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: scratch must be 256-byte aligned");
+
+    std::vector<BtScene> table(n_scenes);
+    uint64_t base = 0, loff = 0;
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        const rt_batch_scene &b = scenes[s];
+        BtScene &e = table[s];
+        std::memset(&e, 0, sizeof(e));
+        e.accel = reinterpret_cast<const uint8_t *>(b.scene.accel);
+        e.tri_material = b.scene.tri_material;
+        e.materials = b.scene.materials;
+        e.lights = b.scene.lights;
+        e.accum = reinterpret_cast<float4 *>(b.accum);
+        e.n_materials = b.scene.n_materials;
+        e.n_lights = b.scene.n_lights;
+        e.light_off = (uint32_t)loff;
+        e.width = b.width;
+        e.height = b.height;
+        e.base = (uint32_t)base;
+        if ((uint64_t)b.width * b.height) camera_aspects(&b.camera, b.width, b.height, &e.ay, &e.ax);
+        e.cam[0] = b.camera.position[0];
+        e.cam[1] = b.camera.position[1];
+        e.cam[2] = b.camera.position[2];
+        base += (uint64_t)b.width * b.height;
+        loff += b.scene.n_lights;
+    }
+    rt_batch_plan *pl = new rt_batch_plan();
+    pl->ctx = ctx;
+    pl->n_scenes = n_scenes;
+    pl->p = *p;
+    pl->t = tt;
+    pl->flags = flags;
+    pl->L = L;
+    pl->scratch = static_cast<uint8_t *>(scratch);
+    pl->paths = P;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess && n_scenes)
+        e = cudaMemcpy(pl->scratch + L.table, table.data(), table.size() * sizeof(BtScene), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete pl;
+        return set_cuda_error(ctx, e, "rt_batch_plan_create: scene table upload");
+    }
+    // Load every kernel the launches use (and size the grid-stride grids)
+    // before a capture begins, so that nothing is loaded while capturing.
+    {
+        const void *kernels[] = {(const void *)k_bt_setup, (const void *)k_bt_raygen, (const void *)k_bt_accumulate,
+                                 (const void *)k_bt_sample, (const void *)k_pt_shade<true>, (const void *)k_pt_resolve};
+        cudaFuncAttributes fa;
+        for (const void *k : kernels)
+            if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
+        if (e == cudaSuccess) {
+            resident_blocks(ctx, (const void *)k_pt_shade<true>, (int)tt.shade_threads, 1u);
+            resident_blocks(ctx, (const void *)k_pt_resolve, (int)tt.shade_threads, 1u);
+            const TraceShape shape{tt.trace_threads, tt.trace_blocks_per_sm, tt.stack_ring, tt.refill};
+            rc = prepare_queue_trace_multi(ctx, shape);
+            if (rc) {
+                delete pl;
+                return rc;
+            }
+        }
+        if (e != cudaSuccess) {
+            delete pl;
+            return set_cuda_error(ctx, e, "rt_batch_plan_create: kernel attributes");
+        }
+    }
+    if ((flags & RT_BATCH_GRAPH) && P) {
+        cudaStream_t cs = nullptr;
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = batch_enqueue(pl, cs, &pl->kernels);
+            cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+            if (rc == RT_OK && e2 != cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess && rc == RT_OK) e = cudaGraphInstantiate(&pl->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (cs) cudaStreamDestroy(cs);
+        if (rc != RT_OK || e != cudaSuccess) {
+            if (pl->exec) cudaGraphExecDestroy(pl->exec);
+            delete pl;
+            (void)cudaGetLastError();
+            return rc != RT_OK ? rc : set_cuda_error(ctx, e, "rt_batch_plan_create: graph capture");
+        }
+    } else {
+        // count the launches of one direct enqueue without issuing it
+        const uint64_t waves = P ? (P + cap - 1u) / cap : 0u;
+        pl->kernels = P ? (uint32_t)(2u + (uint64_t)p->spp * waves * (2u + 4u * p->max_depth)) : 0u;
+    }
+    *plan = pl;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_launch(rt_batch_plan *pl, rt_stream stream, uint32_t sample_offset) {
+    if (!pl) return RT_ERR_INVALID_ARG;
+    rt_context *ctx = pl->ctx;
+    if (pl->paths == 0) return RT_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+    if (!pl->sample_known || pl->next_sample != sample_offset) {
+        uint32_t *cnt = reinterpret_cast<uint32_t *>(pl->scratch + pl->L.counters);
+        k_bt_sample<<<1, 32, 0, st>>>(cnt + kCntSample, sample_offset, 0u);
+        RT_CUDA_CTX(ctx, cudaGetLastError());
+    }
+    if (pl->exec) {
+        RT_CUDA_CTX(ctx, cudaGraphLaunch(pl->exec, st));
+    } else {
+        uint32_t k = 0;
+        int rc = batch_enqueue(pl, st, &k);
+        if (rc) return rc;
+    }
+    pl->sample_known = true;
+    pl->next_sample = sample_offset + pl->p.spp;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_ray_counts(rt_batch_plan *pl, rt_stream stream, uint64_t *extension_rays,
+                                         uint64_t *shadow_rays) {
+    if (!pl) return RT_ERR_INVALID_ARG;
+    rt_context *ctx = pl->ctx;
+    unsigned long long h[2] = {0ull, 0ull};
+    if (pl->paths) {
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        RT_CUDA_CTX(ctx, cudaMemcpyAsync(h, pl->scratch + pl->L.counters + kCntRays * 4u, sizeof(h),
+                                         cudaMemcpyDeviceToHost, st));
+        RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
+    }
+    if (extension_rays) *extension_rays = h[0];
+    if (shadow_rays) *shadow_rays = h[1];
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_plan_launches(const rt_batch_plan *pl, uint32_t *kernels) {
+    if (!pl || !kernels) return RT_ERR_INVALID_ARG;
+    *kernels = pl->kernels;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_plan_destroy(rt_batch_plan *pl) {
+    if (!pl) return RT_OK;
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    delete pl;
     return RT_OK;
 }

@@ -5,14 +5,11 @@
 // RT cores inside the driver.  The GB300 has no RT cores, so traversal runs
 // on the SMs:
 //
-//   k_trace_blas    persistent warps over a ray array.  A warp refills its
-//                   idle lanes from a global counter (atomic work stealing)
-//                   whenever enough of them have finished; each lane walks
-//                   the compressed BVH8 with 16-byte node loads and keeps its
-//                   traversal stack in a shared-memory ring whose bottom
-//                   spills to local memory.
-//                   Two-level structures (instances) take a per-thread path
-//                   in the same kernel, chosen on the device from the header.
+//   k_trace_blas (rt_traverse.cuh)  persistent warps over a ray array
+//                   with atomic work stealing and a shared-memory stack ring.
+//   k_trace_tlas    two-level structures (instances): one ray per thread.
+//                   Both kernels are launched; each returns at once when the
+//                   structure in the header is not its kind.
 //   k_pipeline      the sample's raygen + traceRayEXT + closest-hit / miss +
 //                   imageStore, one thread per launch id.
 //
@@ -25,25 +22,11 @@
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"
+#include "rt_traverse.cuh"
 
 namespace rtc {
 
 namespace {
-
-constexpr int kTraceThreads = 128;
-constexpr int kRing = 16;      // shared-memory stack entries per thread
-constexpr int kMaxDepth = 64;  // total stack entries per thread
-constexpr uint32_t kNone = 0xffffffffu;
-
-struct Hit {
-    float t, u, v;
-    uint32_t rec;     // leaf-record index of the best triangle
-    uint32_t tri;     // build-input triangle index
-    uint32_t inst;    // instance index (0 for a bare BLAS)
-    bool found;
-};
-
-__device__ __forceinline__ uint4 ldg4(const uint4 *p) { return __ldg(p); }
 
 __device__ __forceinline__ bool key_less(float t, uint64_t key, float bt, uint64_t bkey) {
     return t < bt || (t == bt && key < bkey);
@@ -240,201 +223,6 @@ __device__ bool trace_ray(const uint8_t *accel, const float o[3], const float d[
     return h.found;
 }
 
-// ---------------------------------------------------------------------------
-// Persistent BLAS traversal (batch API hot path)
-// ---------------------------------------------------------------------------
-
-struct BatchArgs {
-    const uint8_t *accel;
-    const float4 *rays;      // 2 float4 per ray
-    float4 *hits;            // closest: 1 float4 per ray (t, prim bits, u, v)
-    rt_hit_ext *hits_ext;    // nullable
-    uint8_t *occluded;       // any-hit output
-    uint32_t n;
-    uint32_t refill;         // refill when at least this many lanes are idle
-    uint32_t *counter;
-    uint32_t *err;
-    unsigned long long *stats;
-    const uint32_t *n_dev;   // when set: the ray count, read on the device
-    uint32_t out_rec;        // closest hit: write the leaf-record index
-};
-
-template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_blas(const BatchArgs a) {
-    __shared__ uint2 s_stack[kRing][kTraceThreads];
-    const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
-    const uint4 *nodes = reinterpret_cast<const uint4 *>(a.accel + hd->node_offset);
-    const uint4 *prims = reinterpret_cast<const uint4 *>(a.accel + hd->prim_offset);
-    const bool empty = hd->prim_count == 0;
-    const int tid = threadIdx.x, lane = tid & 31;
-    if (hd->kind != RT_ACCEL_KIND_BLAS) return;  // k_trace_tlas handles it
-
-    bool active = false, exhausted = false;
-    uint32_t ray_idx = 0;
-    Ray r;
-    float tmin = 0.f;
-    Hit h;
-    h.t = 0.f; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.inst = 0; h.found = false;
-    uint32_t node = 0;
-    bool pending = false;
-    uint2 g = make_uint2(0u, 0u);
-    int sp = 0, lo = 0;
-    uint2 spill[kMaxDepth];
-    unsigned long long n_nodes = 0, n_tris = 0;
-    // A tree walk visits each node at most once: more visits, or a node index
-    // past the end, can only come from a corrupt structure.
-    const uint32_t max_visits = hd->node_count;
-    uint32_t visits = 0;
-    const uint32_t n_rays = a.n_dev ? min(*a.n_dev, a.n) : a.n;
-
-    for (;;) {
-        // ---- refill idle lanes from the global counter
-        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-        if (!exhausted && __popc(idle) >= (int)a.refill) {
-            const uint32_t cnt = __popc(idle);
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(a.counter, cnt);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base + cnt >= n_rays) exhausted = true;
-            if (!active) {
-                const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
-                if (idx < n_rays) {
-                    const float4 r0 = __ldg(a.rays + 2u * idx), r1 = __ldg(a.rays + 2u * idx + 1u);
-                    const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
-                    ray_setup(r, o, d);
-                    tmin = r0.w;
-                    h.t = r1.w; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.found = false;
-                    ray_idx = idx;
-                    active = true;
-                    node = 0;          // start at the root
-                    visits = 0;
-                    pending = !empty;  // an empty structure resolves as a miss
-                    g = make_uint2(0u, 0u);
-                    sp = 0;
-                    lo = 0;
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) {
-            if (exhausted) break;
-            continue;
-        }
-        // ---- traversal steps until too many lanes are idle
-        for (;;) {
-            if (active) {
-                bool finish = false;
-                if (pending && (visits >= max_visits || node >= max_visits)) {
-                    report_error(a.err, RT_ERR_BOUNDS, 0x76000000u | ray_idx);
-                    pending = false;
-                    finish = true;
-                }
-                if (pending) {
-                    pending = false;
-                    ++visits;
-                    NodeWords nd = load_node(nodes, node);
-                    uint32_t nh, ph;
-                    isect_node(r, nd, tmin, h.t, nh, ph);
-                    if (STATS) n_nodes++;
-                    const uint32_t pbase = nd.w1.y;
-                    while (ph) {
-                        const uint32_t i = __ffs(ph) - 1;
-                        ph &= ph - 1u;
-                        const uint4 *rec = prims + (size_t)(pbase + i) * 3u;
-                        const uint4 q0 = ldg4(rec), q1 = ldg4(rec + 1), q2 = ldg4(rec + 2);
-                        if (STATS) n_tris++;
-                        float t, u, v;
-                        if (!isect_tri(r,
-                                       make_float4(__uint_as_float(q0.x), __uint_as_float(q0.y),
-                                                   __uint_as_float(q0.z), 0.f),
-                                       make_float4(__uint_as_float(q1.x), __uint_as_float(q1.y),
-                                                   __uint_as_float(q1.z), 0.f),
-                                       make_float4(__uint_as_float(q2.x), __uint_as_float(q2.y),
-                                                   __uint_as_float(q2.z), 0.f),
-                                       tmin, h.t, t, u, v))
-                            continue;
-                        if (ANY) {
-                            h.t = t; h.found = true;
-                            finish = true;
-                            break;
-                        }
-                        if (t < h.t || (t == h.t && q0.w < h.tri)) {
-                            h.t = t; h.u = u; h.v = v; h.rec = pbase + i; h.tri = q0.w; h.found = true;
-                        }
-                    }
-                    g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
-                }
-                // ---- next node: from the current group, else pop
-                while (!finish) {
-                    if (g.y & 0xffu) {
-                        const uint32_t k = __ffs(g.y & 0xffu) - 1;
-                        g.y &= ~(1u << k);
-                        const uint32_t s = k ^ r.oct;
-                        node = g.x + __popc((g.y >> 8) & ((1u << s) - 1u));
-                        pending = true;
-                        if (g.y & 0xffu) {
-                            if (sp >= kMaxDepth) {
-                                report_error(a.err, RT_ERR_BOUNDS, 0x72000000u | ray_idx);
-                                finish = true;
-                                break;
-                            }
-                            if (sp - lo == kRing) {
-                                spill[lo] = s_stack[lo & (kRing - 1)][tid];
-                                ++lo;
-                            }
-                            s_stack[sp & (kRing - 1)][tid] = g;
-                            ++sp;
-                        }
-                        break;
-                    }
-                    if (sp == 0) { finish = true; break; }
-                    --sp;
-                    if (sp >= lo) {
-                        g = s_stack[sp & (kRing - 1)][tid];
-                    } else {
-                        g = spill[sp];
-                        lo = sp;
-                    }
-                }
-                if (finish) {
-                    // ---- write the result
-                    if (ANY) {
-                        if (a.occluded) a.occluded[ray_idx] = h.found ? 1u : 0u;
-                    } else {
-                        float4 out;
-                        if (h.found) out = make_float4(h.t, __uint_as_float(a.out_rec ? h.rec : h.tri), h.u, h.v);
-                        else out = make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
-                        if (a.hits) a.hits[ray_idx] = out;
-                        if (a.hits_ext) {
-                            rt_hit_ext x;
-                            x.t = out.x; x.u = out.z; x.v = out.w;
-                            x.instance_id = h.found ? 0u : kNone;
-                            x.custom_index = 0;
-                            x.geometry_index = h.found ? ldg4(prims + (size_t)h.rec * 3u + 1).w : 0u;
-                            x.primitive_id = h.found ? ldg4(prims + (size_t)h.rec * 3u + 2).w : kNone;
-                            x.sbt_record = x.geometry_index;
-                            a.hits_ext[ray_idx] = x;
-                        }
-                    }
-                    active = false;
-                    pending = false;
-                }
-            }
-            const uint32_t act = __ballot_sync(0xffffffffu, active);
-            if (act == 0u) break;
-            if (!exhausted && (uint32_t)__popc(~act) >= a.refill) break;
-        }
-    }
-    if (STATS) {
-        for (int o = 16; o > 0; o >>= 1) {
-            n_nodes += __shfl_xor_sync(0xffffffffu, n_nodes, o);
-            n_tris += __shfl_xor_sync(0xffffffffu, n_tris, o);
-        }
-        if (lane == 0) {
-            atomicAdd(a.stats, n_nodes);
-            atomicAdd(a.stats + 1, n_tris);
-        }
-    }
-}
 
 // Two-level structures (instances): one ray per thread, grid-stride, through
 // the per-thread path.  Launched beside k_trace_blas; each kernel returns at
@@ -560,7 +348,7 @@ __global__ void __launch_bounds__(128) k_pipeline(const PipelineArgs a) {
 int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *rays, rt_hit *hits,
                  rt_hit_ext *hits_ext, uint8_t *occ, uint32_t n, bool any, unsigned long long *stats) {
     if (n == 0) return RT_OK;
-    BatchArgs a;
+    BatchArgs a{};
     a.accel = reinterpret_cast<const uint8_t *>(accel);
     a.rays = reinterpret_cast<const float4 *>(rays);
     a.hits = reinterpret_cast<float4 *>(hits);
@@ -584,18 +372,18 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     const uint32_t tl_blocks = (uint32_t)ctx->sm_count * 4u < need ? (uint32_t)ctx->sm_count * 4u : need;
     if (stats) {
         if (any) {
-            k_trace_blas<true, true><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_blas<true, true, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
             k_trace_tlas<true, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         } else {
-            k_trace_blas<false, true><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_blas<false, true, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
             k_trace_tlas<false, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         }
     } else {
         if (any) {
-            k_trace_blas<true, false><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_blas<true, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
             k_trace_tlas<true, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         } else {
-            k_trace_blas<false, false><<<blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_blas<false, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
             k_trace_tlas<false, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         }
     }
@@ -613,7 +401,7 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
 int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
                        uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any) {
     if (max_n == 0) return RT_OK;
-    BatchArgs a;
+    BatchArgs a{};
     a.accel = accel;
     a.rays = static_cast<const float4 *>(rays);
     a.hits = static_cast<float4 *>(hits);
@@ -631,8 +419,8 @@ int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, c
     uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
     uint32_t need = (max_n + kTraceThreads - 1) / kTraceThreads;
     if (blocks > need) blocks = need;
-    if (any) k_trace_blas<true, false><<<blocks, kTraceThreads, 0, st>>>(a);
-    else k_trace_blas<false, false><<<blocks, kTraceThreads, 0, st>>>(a);
+    if (any) k_trace_blas<true, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
+    else k_trace_blas<false, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }

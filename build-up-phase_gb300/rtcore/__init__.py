@@ -32,9 +32,13 @@ RT_ERR_TIMEOUT = -4
 RT_ERR_BOUNDS = -5
 RT_ERR_UNSUPPORTED = -6
 RT_ERR_NO_DEVICE = -7
+RT_ERR_NOT_FOUND = -8
 STATUS_NAMES = {0: "RT_OK", -1: "RT_ERR_INVALID_ARG", -2: "RT_ERR_OOM", -3: "RT_ERR_CUDA",
                 -4: "RT_ERR_TIMEOUT", -5: "RT_ERR_BOUNDS", -6: "RT_ERR_UNSUPPORTED",
-                -7: "RT_ERR_NO_DEVICE"}
+                -7: "RT_ERR_NO_DEVICE", -8: "RT_ERR_NOT_FOUND"}
+RT_BATCH_GRAPH = 1
+RT_BATCH_DISCARD = 2
+RT_TUNE_FORCE = 1
 
 RT_INDEX_NONE = 0
 RT_INDEX_UINT32 = 1
@@ -131,6 +135,28 @@ class PtCacheParams(C.Structure):
     _fields_ = [("cache", C.c_void_p), ("train_paths", C.c_uint32), ("train_batch", C.c_uint32)]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("scene", PtScene), ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("accum", C.c_void_p)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("max_depth", C.c_uint32), ("rr_depth", C.c_uint32), ("flags", C.c_uint32),
+                ("seed", C.c_uint64), ("ray_eps", C.c_float), ("reserved", C.c_uint32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("trace_threads", C.c_uint32), ("trace_blocks_per_sm", C.c_uint32), ("stack_ring", C.c_uint32),
+                ("refill", C.c_uint32), ("shade_threads", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("bvh_width", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+assert C.sizeof(BatchScene) == 80
+assert C.sizeof(BatchParams) == 32
+assert C.sizeof(BatchTuning) == 32
 assert C.sizeof(PtLight) == 48
 assert C.sizeof(GeometryTriangles) == 48
 assert C.sizeof(Instance) == 64
@@ -172,6 +198,21 @@ PROTOTYPES = {
     "rt_pt_cached_scratch_bytes": (_i32, [C.POINTER(PtParams), C.POINTER(PtCacheParams), C.POINTER(_u64)]),
     "rt_path_trace_cached": (_i32, [_vp, _vp, C.POINTER(PtScene), C.POINTER(PtParams), C.POINTER(PtCacheParams), _vp,
                                     _vp, _u64]),
+    # batched path tracing and its autotuner declared in include/rtcore_batch.h
+    "rt_batch_default_tuning": (_i32, [C.POINTER(BatchTuning)]),
+    "rt_batch_scratch_bytes": (_i32, [C.POINTER(BatchScene), _u32, C.POINTER(BatchParams), C.POINTER(BatchTuning),
+                                      C.POINTER(_u64)]),
+    "rt_batch_plan_create": (_i32, [_vp, C.POINTER(BatchScene), _u32, C.POINTER(BatchParams),
+                                    C.POINTER(BatchTuning), _vp, _u64, _u32, C.POINTER(_vp)]),
+    "rt_batch_launch": (_i32, [_vp, _vp, _u32]),
+    "rt_batch_ray_counts": (_i32, [_vp, _vp, C.POINTER(_u64), C.POINTER(_u64)]),
+    "rt_batch_plan_launches": (_i32, [_vp, C.POINTER(_u32)]),
+    "rt_batch_plan_destroy": (_i32, [_vp]),
+    "rt_batch_autotune": (_i32, [_vp, C.POINTER(BatchScene), _u32, C.POINTER(BatchParams), _vp, _u64, C.c_char_p,
+                                 _u32, C.POINTER(BatchTuning), C.POINTER(_f)]),
+    "rt_batch_tuning_key": (_i32, [_vp, C.POINTER(BatchScene), _u32, C.POINTER(BatchParams), C.c_char_p, _u32]),
+    "rt_batch_tuning_cache_lookup": (_i32, [C.c_char_p, C.c_char_p, C.POINTER(BatchTuning), C.POINTER(_f)]),
+    "rt_batch_tuning_cache_store": (_i32, [C.c_char_p, C.c_char_p, C.POINTER(BatchTuning), _f]),
     # MLP radiance cache declared in include/rtcore_cache.h
     "rt_cache_bytes": (_i32, [C.POINTER(_u64)]),
     "rt_cache_param_count": (_u32, []),
@@ -365,6 +406,43 @@ class Context:
                                              C.byref(e), C.byref(s)), "rt_pt_ray_counts")
         return e.value, s.value
 
+    # ---- batched path tracing
+    def batch_scratch_bytes(self, scenes, params: BatchParams, tuning: "BatchTuning | None" = None) -> int:
+        arr = _scene_array(scenes)
+        out = C.c_uint64()
+        self.check(self.lib.rt_batch_scratch_bytes(arr, len(arr), C.byref(params),
+                                                   C.byref(tuning) if tuning is not None else None, C.byref(out)),
+                   "rt_batch_scratch_bytes")
+        return out.value
+
+    def batch_plan(self, scenes, params: BatchParams, scratch, scratch_bytes: int,
+                   tuning: "BatchTuning | None" = None, graph: bool = True, discard: bool = False) -> "BatchPlan":
+        arr = _scene_array(scenes)
+        h = C.c_void_p()
+        flags = (RT_BATCH_GRAPH if graph else 0) | (RT_BATCH_DISCARD if discard else 0)
+        self.check(self.lib.rt_batch_plan_create(self.h, arr, len(arr), C.byref(params),
+                                                 C.byref(tuning) if tuning is not None else None, _ptr(scratch),
+                                                 scratch_bytes, flags, C.byref(h)), "rt_batch_plan_create")
+        return BatchPlan(self, h)
+
+    def batch_autotune(self, scenes, params: BatchParams, scratch, scratch_bytes: int, cache_path=None,
+                       force: bool = False):
+        """(BatchTuning, ms of one sample per pixel) chosen by the autotuner."""
+        arr = _scene_array(scenes)
+        t, ms = BatchTuning(), C.c_float()
+        path = os.fsencode(str(cache_path)) if cache_path is not None else None
+        self.check(self.lib.rt_batch_autotune(self.h, arr, len(arr), C.byref(params), _ptr(scratch), scratch_bytes,
+                                              path, RT_TUNE_FORCE if force else 0, C.byref(t), C.byref(ms)),
+                   "rt_batch_autotune")
+        return t, ms.value
+
+    def batch_tuning_key(self, scenes, params: BatchParams) -> str:
+        arr = _scene_array(scenes)
+        buf = C.create_string_buffer(160)
+        self.check(self.lib.rt_batch_tuning_key(self.h, arr, len(arr), C.byref(params), buf, len(buf)),
+                   "rt_batch_tuning_key")
+        return buf.value.decode()
+
     # ---- MLP radiance cache
     def cache_bytes(self) -> int:
         out = C.c_uint64()
@@ -398,6 +476,68 @@ class Context:
     def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:
         self.check(self.lib.rt_sort_pairs(self.h, _stream_ptr(stream), _ptr(keys), _ptr(vals), n, key_bits,
                                           _ptr(scratch), scratch_bytes), "rt_sort_pairs")
+
+
+def _scene_array(scenes):
+    if isinstance(scenes, C.Array):
+        return scenes
+    scenes = list(scenes)
+    return (BatchScene * len(scenes))(*scenes)
+
+
+class BatchPlan:
+    """rt_batch_plan: one recorded launch of a batch of scenes."""
+
+    def __init__(self, ctx: Context, h: C.c_void_p):
+        self.ctx, self.h = ctx, h
+
+    def launch(self, sample_offset: int, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.rt_batch_launch(self.h, _stream_ptr(stream), sample_offset), "rt_batch_launch")
+
+    def ray_counts(self, stream=None):
+        e, s = C.c_uint64(), C.c_uint64()
+        self.ctx.check(self.ctx.lib.rt_batch_ray_counts(self.h, _stream_ptr(stream), C.byref(e), C.byref(s)),
+                       "rt_batch_ray_counts")
+        return e.value, s.value
+
+    def launches(self) -> int:
+        k = C.c_uint32()
+        self.ctx.check(self.ctx.lib.rt_batch_plan_launches(self.h, C.byref(k)), "rt_batch_plan_launches")
+        return k.value
+
+    def close(self) -> None:
+        if self.h:
+            self.ctx.lib.rt_batch_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_batch_tuning() -> BatchTuning:
+    t = BatchTuning()
+    load().rt_batch_default_tuning(C.byref(t))
+    return t
+
+
+def tuning_cache_lookup(path, key: str):
+    """(BatchTuning, ms) for key, or None when the file or key is absent."""
+    t, ms = BatchTuning(), C.c_float()
+    rc = load().rt_batch_tuning_cache_lookup(os.fsencode(str(path)), key.encode(), C.byref(t), C.byref(ms))
+    if rc == RT_ERR_NOT_FOUND:
+        return None
+    if rc != RT_OK:
+        raise RtError(rc, "rt_batch_tuning_cache_lookup")
+    return t, ms.value
+
+
+def tuning_cache_store(path, key: str, t: BatchTuning, ms: float) -> None:
+    rc = load().rt_batch_tuning_cache_store(os.fsencode(str(path)), key.encode(), C.byref(t), ms)
+    if rc != RT_OK:
+        raise RtError(rc, "rt_batch_tuning_cache_store")
 
 
 def sort_scratch_bytes(n: int, key_bits: int) -> int:
