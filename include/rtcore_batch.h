@@ -106,9 +106,10 @@ rt_status rt_batch_plan_destroy(rt_batch_plan *plan);
 
 /*
  * Autotuner.  Times candidate tunings on this batch (one sample per pixel,
- * graph launches, CUDA events, the best of two launches after a warm-up),
+ * graph launches, CUDA events, the best of three launches after a warm-up),
  * walking one parameter at a time from the defaults and keeping each
- * improvement, and returns the fastest in *best (its time in *best_ms).
+ * improvement of more than 1 %, and returns the fastest in *best (its time in
+ * *best_ms).
  * With a cache_path, the result is looked up first and stored after tuning
  * in a JSON file keyed by rt_batch_tuning_key; flags RT_TUNE_FORCE re-tunes
  * even when the key is present.  scratch: rt_batch_scratch_bytes(..., NULL).
