@@ -8,13 +8,18 @@
 // librtcore, without a window: one frame (or --frames N timed frames) into an
 // RGBA32F device buffer, written out as PPM (and PFM).
 //
-//   rt_sample [--scene ref8|tri] [--width W] [--height H] [--out F.ppm]
-//             [--pfm F.pfm] [--raw F.bin] [--frames N]
+//   rt_sample [--scene ref8|tri] [--obj F.obj] [--camera X Y Z FOV]
+//             [--width W] [--height H] [--out F.ppm] [--pfm F.pfm]
+//             [--raw F.bin] [--frames N]
 //
 // --scene ref8: the sample's own scene and camera (1200x800, camera (0,0,10),
 //               two geometries x two instances, SBT colours, sample chit);
 // --scene tri : one triangle (-1,-1,0),(1,-1,0),(0,1,0), camera (0,0,2.5),
 //               800x600, barycentric closest hit.
+// --obj F     : the mesh of a Wavefront OBJ file (rt_obj_load) as one
+//               geometry under one identity instance, barycentric closest
+//               hit, 800x600; the camera looks down -z at the mesh from in
+//               front of its bounds unless --camera gives it.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -25,6 +30,7 @@
 #include <vector>
 
 #include "rtcore.h"
+#include "rtcore_scene.h"
 
 namespace {
 
@@ -56,8 +62,10 @@ T *upload(const T *host, size_t n) {
 }  // namespace
 
 int main(int argc, char **argv) {
-    std::string scene = "ref8", out_ppm = "rt_sample.ppm", out_pfm, out_raw;
+    std::string scene = "ref8", out_ppm = "rt_sample.ppm", out_pfm, out_raw, obj;
     uint32_t width = 0, height = 0;
+    bool cam_given = false;
+    float cam_arg[4] = {0.0f, 0.0f, 0.0f, 60.0f};
     int frames = 1;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
@@ -69,13 +77,18 @@ int main(int argc, char **argv) {
         else if (a == "--pfm") out_pfm = next();
         else if (a == "--raw") out_raw = next();
         else if (a == "--frames") frames = std::atoi(next());
+        else if (a == "--obj") { obj = next(); scene = "obj"; }
+        else if (a == "--camera") {
+            for (int k = 0; k < 4; ++k) cam_arg[k] = (float)std::atof(next());
+            cam_given = true;
+        }
         else {
             std::fprintf(stderr, "unknown argument %s\n", a.c_str());
             return 2;
         }
     }
     const bool ref8 = scene == "ref8";
-    if (!ref8 && scene != "tri") {
+    if (!ref8 && scene != "tri" && scene != "obj") {
         std::fprintf(stderr, "--scene must be ref8 or tri\n");
         return 2;
     }
@@ -102,6 +115,31 @@ int main(int argc, char **argv) {
         indices = {0, 1, 3, 1, 2, 3};                                  // main.cpp:682
         geo_xf = {{{{1, 0, 0, -2}, {0, 1, 0, 0}, {0, 0, 1, 0}}},       // main.cpp:684-695
                   {{{1, 0, 0, 2}, {0, 1, 0, 0}, {0, 0, 1, 0}}}};
+    } else if (scene == "obj") {
+        uint32_t nv = 0, nt = 0, nm = 0;
+        rt_status s = rt_obj_counts(obj.c_str(), &nv, &nt, &nm);
+        if (s == RT_OK) {
+            vertices.resize((size_t)nv * 3u);
+            indices.resize((size_t)nt * 3u);
+            s = rt_obj_load(obj.c_str(), vertices.data(), indices.data(), nullptr);
+        }
+        if (s != RT_OK || nt == 0) {
+            std::fprintf(stderr, "cannot load %s as an OBJ mesh with triangles (%d)\n", obj.c_str(), s);
+            return 1;
+        }
+        if (!cam_given) {
+            // in front of the bounds (+z), looking -z, 60 degrees
+            float lo[3] = {vertices[0], vertices[1], vertices[2]}, hi[3] = {lo[0], lo[1], lo[2]};
+            for (size_t k = 0; k < vertices.size(); ++k) {
+                lo[k % 3] = vertices[k] < lo[k % 3] ? vertices[k] : lo[k % 3];
+                hi[k % 3] = vertices[k] > hi[k % 3] ? vertices[k] : hi[k % 3];
+            }
+            const float ext = (hi[0] - lo[0]) > (hi[1] - lo[1]) ? (hi[0] - lo[0]) : (hi[1] - lo[1]);
+            cam_arg[0] = 0.5f * (lo[0] + hi[0]);
+            cam_arg[1] = 0.5f * (lo[1] + hi[1]);
+            cam_arg[2] = hi[2] + 1.2f * ext;
+            cam_arg[3] = 60.0f;
+        }
     } else {
         vertices = {-1, -1, 0, 1, -1, 0, 0, 1, 0};
         indices = {0, 1, 2};
@@ -170,6 +208,7 @@ int main(int argc, char **argv) {
 
     // ---- createUniformBuffer (main.cpp:1001-1017)
     rt_camera cam = ref8 ? rt_camera{{0.0f, 0.0f, 10.0f}, 60.0f} : rt_camera{{0.0f, 0.0f, 2.5f}, 60.0f};
+    if (scene == "obj" || cam_given) cam = rt_camera{{cam_arg[0], cam_arg[1], cam_arg[2]}, cam_arg[3]};
 
     // ---- createRayTracingPipeline + createShaderBindingTable (main.cpp:1093-1320)
     rt_pipeline pipe;

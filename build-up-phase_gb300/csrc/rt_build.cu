@@ -160,6 +160,57 @@ __global__ void k_empty_root(uint8_t *accel) {
 // prep
 // ---------------------------------------------------------------------------
 
+// Leaf record and box of triangle p of geometry g (build-input index gi):
+// the three vertices (transformed when the geometry has a transform) in .xyz
+// and the ids in .w; NaN vertices and the empty box for a triangle that is
+// inactive (an index beyond max_vertex, a NaN coordinate).  Shared by the
+// build and the refit.
+__device__ bool tri_record(const GeomParams &gp, uint32_t g, uint32_t p, uint32_t gi, uint4 *r, Box &b,
+                           uint32_t *err, uint32_t *hdr_status) {
+    const rt_geometry_triangles &G = gp.g[g];
+    float v[3][3];
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+        uint32_t idx = G.index_type == RT_INDEX_UINT32 ? G.indices[3u * p + (uint32_t)k] : 3u * p + (uint32_t)k;
+        if (idx > G.max_vertex) {
+            ok = false;
+            report_error(err, RT_ERR_BOUNDS, gi);
+            if (hdr_status) atomicCAS(hdr_status, 0u, (uint32_t)(-RT_ERR_BOUNDS));
+            break;
+        }
+        const float *src = reinterpret_cast<const float *>(reinterpret_cast<const uint8_t *>(G.vertices) +
+                                                           (size_t)idx * G.vertex_stride);
+        float pt[3] = {src[0], src[1], src[2]};
+        if (G.transform) {
+            const float *m = &G.transform->m[0][0];
+            float mm[12];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) mm[q] = __ldg(m + q);
+            xform_point(mm, pt, v[k]);
+        } else {
+            v[k][0] = pt[0]; v[k][1] = pt[1]; v[k][2] = pt[2];
+        }
+    }
+    if (ok)
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a)
+                if (isnan(v[k][a])) ok = false;
+    const float qnan = __int_as_float(0x7fc00000);
+    r[0] = make_uint4(__float_as_uint(ok ? v[0][0] : qnan), __float_as_uint(ok ? v[0][1] : qnan),
+                      __float_as_uint(ok ? v[0][2] : qnan), gi);
+    r[1] = make_uint4(__float_as_uint(ok ? v[1][0] : qnan), __float_as_uint(ok ? v[1][1] : qnan),
+                      __float_as_uint(ok ? v[1][2] : qnan), g);
+    r[2] = make_uint4(__float_as_uint(ok ? v[2][0] : qnan), __float_as_uint(ok ? v[2][1] : qnan),
+                      __float_as_uint(ok ? v[2][2] : qnan), p);
+    b = box_empty();
+    if (ok)
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = fmn(fmn(v[0][a], v[1][a]), v[2][a]);
+            b.hi[a] = fmx(fmx(v[0][a], v[1][a]), v[2][a]);
+        }
+    return ok;
+}
+
 __global__ void __launch_bounds__(256) k_prep_tris(const GeomParams gp, uint32_t n, uint4 *__restrict__ recs,
                                                     float *__restrict__ boxes, int32_t *cbounds, uint32_t *err,
                                                     uint32_t *hdr_status) {
@@ -173,49 +224,9 @@ __global__ void __launch_bounds__(256) k_prep_tris(const GeomParams gp, uint32_t
             if (gp.table[mid] <= gi) lo = mid; else hi = mid;
         }
         const uint32_t g = lo;
-        const rt_geometry_triangles &G = gp.g[g];
         const uint32_t p = gi - gp.table[g];
-        float v[3][3];
-        bool ok = true;
-        for (int k = 0; k < 3; ++k) {
-            uint32_t idx = G.index_type == RT_INDEX_UINT32 ? G.indices[3u * p + (uint32_t)k] : 3u * p + (uint32_t)k;
-            if (idx > G.max_vertex) {
-                ok = false;
-                report_error(err, RT_ERR_BOUNDS, gi);
-                if (hdr_status) atomicCAS(hdr_status, 0u, (uint32_t)(-RT_ERR_BOUNDS));
-                break;
-            }
-            const float *src = reinterpret_cast<const float *>(reinterpret_cast<const uint8_t *>(G.vertices) +
-                                                               (size_t)idx * G.vertex_stride);
-            float pt[3] = {src[0], src[1], src[2]};
-            if (G.transform) {
-                const float *m = &G.transform->m[0][0];
-                float mm[12];
-#pragma unroll
-                for (int q = 0; q < 12; ++q) mm[q] = __ldg(m + q);
-                xform_point(mm, pt, v[k]);
-            } else {
-                v[k][0] = pt[0]; v[k][1] = pt[1]; v[k][2] = pt[2];
-            }
-        }
-        if (ok)
-            for (int k = 0; k < 3; ++k)
-                for (int a = 0; a < 3; ++a)
-                    if (isnan(v[k][a])) ok = false;
-        const float qnan = __int_as_float(0x7fc00000);
-        uint4 *r = recs + (size_t)gi * 3u;
-        r[0] = make_uint4(__float_as_uint(ok ? v[0][0] : qnan), __float_as_uint(ok ? v[0][1] : qnan),
-                          __float_as_uint(ok ? v[0][2] : qnan), gi);
-        r[1] = make_uint4(__float_as_uint(ok ? v[1][0] : qnan), __float_as_uint(ok ? v[1][1] : qnan),
-                          __float_as_uint(ok ? v[1][2] : qnan), g);
-        r[2] = make_uint4(__float_as_uint(ok ? v[2][0] : qnan), __float_as_uint(ok ? v[2][1] : qnan),
-                          __float_as_uint(ok ? v[2][2] : qnan), p);
-        Box b = box_empty();
-        if (ok)
-            for (int a = 0; a < 3; ++a) {
-                b.lo[a] = fmn(fmn(v[0][a], v[1][a]), v[2][a]);
-                b.hi[a] = fmx(fmx(v[0][a], v[1][a]), v[2][a]);
-            }
+        Box b;
+        const bool ok = tri_record(gp, g, p, gi, recs + (size_t)gi * 3u, b, err, hdr_status);
         store_box(boxes, gi, b);
         if (ok)
             for (int a = 0; a < 3; ++a) {
@@ -245,40 +256,47 @@ __device__ bool invert3x4(const float *m, float out[12]) {
     return true;
 }
 
+// Leaf record (world-to-object 3x4, BLAS address, custom index / mask, SBT
+// offset / flags, instance index) and world box of instance i.  Shared by the
+// build and the refit.
+__device__ void inst_record(const rt_instance &I, uint32_t i, uint4 *r, Box &b) {
+    const float *m = &I.transform.m[0][0];
+    float w2o[12];
+    bool ok = invert3x4(m, w2o);
+    if (!ok)
+        for (int q = 0; q < 12; ++q) w2o[q] = 0.0f;
+    const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(I.accel_ref);
+    b = box_empty();
+    if (ok && bh && bh->prim_count > 0) {
+        for (int c = 0; c < 8; ++c) {
+            float pt[3] = {(c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
+                           (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
+                           (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]};
+            float w[3];
+            xform_point(m, pt, w);
+            for (int a = 0; a < 3; ++a) { b.lo[a] = fmn(b.lo[a], w[a]); b.hi[a] = fmx(b.hi[a], w[a]); }
+        }
+    }
+    r[0] = make_uint4(__float_as_uint(w2o[0]), __float_as_uint(w2o[1]), __float_as_uint(w2o[2]),
+                      __float_as_uint(w2o[3]));
+    r[1] = make_uint4(__float_as_uint(w2o[4]), __float_as_uint(w2o[5]), __float_as_uint(w2o[6]),
+                      __float_as_uint(w2o[7]));
+    r[2] = make_uint4(__float_as_uint(w2o[8]), __float_as_uint(w2o[9]), __float_as_uint(w2o[10]),
+                      __float_as_uint(w2o[11]));
+    r[3] = make_uint4((uint32_t)(I.accel_ref & 0xffffffffu), (uint32_t)(I.accel_ref >> 32), I.custom_index_and_mask,
+                      I.sbt_offset_and_flags);
+    r[4] = make_uint4(i, 0u, 0u, 0u);
+}
+
 __global__ void __launch_bounds__(256) k_prep_inst(const rt_instance *__restrict__ inst, uint32_t n,
                                                     uint4 *__restrict__ recs, float *__restrict__ boxes,
                                                     int32_t *cbounds) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     int32_t cmin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, cmax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
     if (i < n) {
-        rt_instance I = inst[i];
-        const float *m = &I.transform.m[0][0];
-        float w2o[12];
-        bool ok = invert3x4(m, w2o);
-        if (!ok)
-            for (int q = 0; q < 12; ++q) w2o[q] = 0.0f;
-        const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(I.accel_ref);
-        Box b = box_empty();
-        if (ok && bh && bh->prim_count > 0) {
-            for (int c = 0; c < 8; ++c) {
-                float pt[3] = {(c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
-                               (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
-                               (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]};
-                float w[3];
-                xform_point(m, pt, w);
-                for (int a = 0; a < 3; ++a) { b.lo[a] = fmn(b.lo[a], w[a]); b.hi[a] = fmx(b.hi[a], w[a]); }
-            }
-        }
-        uint4 *r = recs + (size_t)i * 5u;
-        r[0] = make_uint4(__float_as_uint(w2o[0]), __float_as_uint(w2o[1]), __float_as_uint(w2o[2]),
-                          __float_as_uint(w2o[3]));
-        r[1] = make_uint4(__float_as_uint(w2o[4]), __float_as_uint(w2o[5]), __float_as_uint(w2o[6]),
-                          __float_as_uint(w2o[7]));
-        r[2] = make_uint4(__float_as_uint(w2o[8]), __float_as_uint(w2o[9]), __float_as_uint(w2o[10]),
-                          __float_as_uint(w2o[11]));
-        r[3] = make_uint4((uint32_t)(I.accel_ref & 0xffffffffu), (uint32_t)(I.accel_ref >> 32),
-                          I.custom_index_and_mask, I.sbt_offset_and_flags);
-        r[4] = make_uint4(i, 0u, 0u, 0u);
+        const rt_instance I = inst[i];
+        Box b;
+        inst_record(I, i, recs + (size_t)i * 5u, b);
         store_box(boxes, i, b);
         if (!box_is_empty(b))
             for (int a = 0; a < 3; ++a) {
@@ -550,17 +568,12 @@ __device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, uint32_t &n_
     n_prim = np;
 }
 
-// Phase B: writes wide node k with its child and record bases.
-__device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t child_base, uint32_t prim_base) {
-    const uint32_t src = __ldcg(a.wq + k);
-    const Box node = ref_box(a, src);
-    uint32_t slot_ref[8];
-    Box sbox[8];
-    for (int s = 0; s < 8; ++s) {
-        slot_ref[s] = __ldcg(a.slots + (size_t)k * 8u + s);
-        if (slot_ref[s] != kNone) sbox[s] = ref_box(a, slot_ref[s]);
-        else sbox[s] = box_empty();
-    }
+// Origin, per-axis power-of-two scales and the 8-bit child boxes of a wide
+// node (words 0, 2, 3, 4 of its five; word 1 holds the child and record
+// bases and the slot metadata): the boxes are rounded outward (lower bounds
+// down, upper bounds up) so the quantised box contains the exact one.  Shared
+// by the build and the refit.
+__device__ void encode_node(const Box &node, const Box sbox[8], const bool used[8], uint32_t imask, uint4 *o) {
     const bool empty = box_is_empty(node);
     float p[3];
     int e[3];
@@ -568,11 +581,9 @@ __device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t chi
         p[q] = empty ? 0.0f : node.lo[q];
         e[q] = empty ? 0 : qexp_for(__fsub_ru(node.hi[q], p[q]));
     }
-    uint8_t qlo[3][8], qhi[3][8], meta[8];
-    uint32_t imask = 0, off = 0, ichild = 0;
+    uint8_t qlo[3][8], qhi[3][8];
     for (int s = 0; s < 8; ++s) {
-        const uint32_t r = slot_ref[s];
-        const bool inv = (r == kNone) || empty || box_is_empty(sbox[s]);
+        const bool inv = !used[s] || empty || box_is_empty(sbox[s]);
         for (int q = 0; q < 3; ++q) {
             if (inv) { qlo[q][s] = 255; qhi[q][s] = 0; continue; }
             float sc = pow2f(-e[q]);
@@ -586,6 +597,39 @@ __device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t chi
             qlo[q][s] = (uint8_t)ql;
             qhi[q][s] = (uint8_t)qh;
         }
+    }
+    auto pack4 = [](const uint8_t *b) {
+        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+    };
+    uint32_t w0w = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
+                   ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
+    o[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), w0w);
+    o[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+    o[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+    o[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+}
+
+__device__ __forceinline__ uint32_t pack_meta4(const uint8_t *b) {
+    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+}
+
+// Phase B: writes wide node k with its child and record bases.
+__device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t child_base, uint32_t prim_base) {
+    const uint32_t src = __ldcg(a.wq + k);
+    const Box node = ref_box(a, src);
+    uint32_t slot_ref[8];
+    Box sbox[8];
+    bool used[8];
+    for (int s = 0; s < 8; ++s) {
+        slot_ref[s] = __ldcg(a.slots + (size_t)k * 8u + s);
+        used[s] = slot_ref[s] != kNone;
+        if (used[s]) sbox[s] = ref_box(a, slot_ref[s]);
+        else sbox[s] = box_empty();
+    }
+    uint8_t meta[8];
+    uint32_t imask = 0, off = 0, ichild = 0;
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t r = slot_ref[s];
         meta[s] = 0;
         if (r == kNone) continue;
         if (ref_openable(a, r)) {
@@ -608,17 +652,9 @@ __device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t chi
             off += cnt;
         }
     }
-    auto pack4 = [](const uint8_t *b) {
-        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
-    };
     uint4 *o = a.nodes_out + (size_t)k * 5u;
-    uint32_t w0w = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
-                   ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
-    o[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), w0w);
-    o[1] = make_uint4(child_base, prim_base, pack4(meta), pack4(meta + 4));
-    o[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
-    o[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
-    o[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+    encode_node(node, sbox, used, imask, o);
+    o[1] = make_uint4(child_base, prim_base, pack_meta4(meta), pack_meta4(meta + 4));
 }
 
 template <int N>
@@ -876,6 +912,221 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     return RT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Refit: new leaf records and boxes in the existing topology
+// ---------------------------------------------------------------------------
+//
+// Each leaf record names its primitive (triangle: build-input index,
+// geometry, index in the geometry; instance: instance index), so the records
+// are recomputed in place from the new inputs.  Wide nodes are stored in
+// breadth-first order (every child after its parent); a node's exact box is
+// the union of its slots' boxes -- the union of its primitives' boxes, as in
+// the build, since min/max in a total order do not depend on grouping -- and
+// is quantised by the build's encode_node.  The nodes are walked bottom-up:
+// one thread starts at each node without internal children, and the last of
+// a parent's children to arrive (an atomic counter per node) goes on to the
+// parent.
+
+struct RefitLayout {
+    uint64_t flag, leaf_box, node_box, parent, arrive, total;
+};
+
+RefitLayout refit_layout(uint32_t n) {
+    RefitLayout L;
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t o = off;
+        off += align_up(bytes > 0 ? bytes : 1, 256);
+        return o;
+    };
+    const uint64_t cap = node_capacity_for(n);
+    L.flag = take(16);
+    L.leaf_box = take((uint64_t)n * 24u);
+    L.node_box = take(cap * 24u);
+    L.parent = take(cap * 4u);
+    L.arrive = take(cap * 4u);
+    L.total = off;
+    return L;
+}
+
+// The structure must be the one the inputs describe.
+__global__ void k_refit_begin(const rt_accel_header *h, uint32_t kind, uint32_t n, uint32_t n_geoms, uint32_t cap,
+                              uint32_t *flag, uint32_t *err) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const bool ok = h->magic == RT_ACCEL_MAGIC && h->kind == kind && h->prim_count == n &&
+                    (kind != RT_ACCEL_KIND_BLAS || h->geom_count == n_geoms) && h->node_capacity == cap &&
+                    h->node_count >= 1u && h->node_count <= cap && h->node_offset == RT_ACCEL_HEADER_BYTES &&
+                    h->prim_offset == RT_ACCEL_HEADER_BYTES + (uint64_t)cap * 80u;
+    *flag = ok ? 1u : 0u;
+    if (!ok) report_error(err, RT_ERR_INVALID_ARG, 0x68000000u);
+}
+
+__global__ void __launch_bounds__(256) k_refit_links(const uint4 *nodes, const rt_accel_header *h, uint32_t cap,
+                                                      const uint32_t *flag, uint32_t *parent, uint32_t *arrive,
+                                                      uint32_t *err) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cap || *flag == 0u) return;
+    const uint32_t nc = h->node_count;
+    if (k >= nc) return;
+    arrive[k] = 0u;
+    const uint32_t imask = nodes[(size_t)k * 5u].w >> 24;
+    const uint32_t cb = nodes[(size_t)k * 5u + 1u].x;
+    const uint32_t ni = (uint32_t)__popc(imask);
+    for (uint32_t j = 0; j < ni; ++j) {
+        const uint32_t c = cb + j;
+        if (c <= k || c >= nc) {  // children follow their parent in breadth-first order
+            report_error(err, RT_ERR_BOUNDS, 0x69000000u | (k & 0xffffffu));
+            return;
+        }
+        parent[c] = k;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_refit_tris(const GeomParams gp, uint32_t n, uint4 *recs, float *leaf_box,
+                                                     const uint32_t *flag, uint32_t *err, uint32_t *hdr_status) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n || *flag == 0u) return;
+    uint4 *rec = recs + (size_t)r * 3u;
+    const uint32_t gi = rec[0].w, g = rec[1].w, p = rec[2].w;
+    Box b = box_empty();
+    if (g < gp.n_geoms && p < gp.g[g].tri_count && gi == gp.table[g] + p)
+        tri_record(gp, g, p, gi, rec, b, err, hdr_status);
+    else
+        report_error(err, RT_ERR_BOUNDS, 0x6a000000u | (r & 0xffffffu));
+    store_box(leaf_box, r, b);
+}
+
+__global__ void __launch_bounds__(256) k_refit_inst(const rt_instance *inst, uint32_t n, uint4 *recs,
+                                                     float *leaf_box, const uint32_t *flag, uint32_t *err) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n || *flag == 0u) return;
+    uint4 *rec = recs + (size_t)r * 5u;
+    const uint32_t i = rec[4].x;
+    Box b = box_empty();
+    if (i < n) {
+        const rt_instance I = inst[i];
+        inst_record(I, i, rec, b);
+    } else {
+        report_error(err, RT_ERR_BOUNDS, 0x6b000000u | (r & 0xffffffu));
+    }
+    store_box(leaf_box, r, b);
+}
+
+__global__ void __launch_bounds__(256) k_refit_nodes(uint4 *nodes, rt_accel_header *h, uint32_t cap, uint32_t n,
+                                                      const float *leaf_box, float *node_box, const uint32_t *parent,
+                                                      uint32_t *arrive, const uint32_t *flag, uint32_t *err) {
+    const uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 >= cap || *flag == 0u) return;
+    const uint32_t nc = h->node_count;
+    if (k0 >= nc || (__ldcg(nodes + (size_t)k0 * 5u).w >> 24) != 0u) return;  // start below every internal child
+    uint32_t k = k0;
+    for (int step = 0;; ++step) {
+        if (step >= 256) {  // deeper than any build makes: a corrupt structure
+            report_error(err, RT_ERR_BOUNDS, 0x6c000000u | (k & 0xffffffu));
+            return;
+        }
+        uint4 *o = nodes + (size_t)k * 5u;
+        const uint4 w0 = __ldcg(o), w1 = __ldcg(o + 1);
+        const uint32_t imask = w0.w >> 24, cb = w1.x, pb = w1.y;
+        Box sbox[8];
+        bool used[8];
+        Box node = box_empty();
+        for (int s = 0; s < 8; ++s) {
+            const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
+            used[s] = meta != 0u;
+            sbox[s] = box_empty();
+            if ((imask >> s) & 1u) {
+                const uint32_t c = cb + (uint32_t)__popc(imask & ((1u << s) - 1u));
+                if (c < nc) sbox[s] = load_box(node_box, c);
+                else report_error(err, RT_ERR_BOUNDS, 0x6d000000u | (k & 0xffffffu));
+            } else if (meta) {
+                const uint32_t cnt = (uint32_t)__popc(meta >> 5), first = pb + (meta & 0x1fu);
+                if (first + cnt <= n) {
+                    for (uint32_t j = 0; j < cnt; ++j) sbox[s] = box_union(sbox[s], load_box(leaf_box, first + j));
+                } else {
+                    report_error(err, RT_ERR_BOUNDS, 0x6e000000u | (k & 0xffffffu));
+                }
+            }
+            if (used[s]) node = box_union(node, sbox[s]);
+        }
+        encode_node(node, sbox, used, imask, o);
+        store_box(node_box, k, node);
+        if (k == 0u) {
+            for (int q = 0; q < 3; ++q) { h->bounds_lo[q] = node.lo[q]; h->bounds_hi[q] = node.hi[q]; }
+            return;
+        }
+        __threadfence();  // the box is visible before the arrival is counted
+        const uint32_t p = parent[k];
+        if (p >= k) {  // the root, or a node no parent claimed
+            report_error(err, RT_ERR_BOUNDS, 0x6f000000u | (k & 0xffffffu));
+            return;
+        }
+        const uint32_t need = (uint32_t)__popc(__ldcg(nodes + (size_t)p * 5u).w >> 24);
+        if (atomicAdd(arrive + p, 1u) + 1u != need) return;
+        __threadfence();
+        k = p;
+    }
+}
+
+int run_refit(rt_context *ctx, cudaStream_t st, uint32_t kind, uint32_t n, uint32_t n_geoms, const GeomParams *gp,
+              const rt_instance *instances, void *accel, uint64_t accel_bytes, void *scratch,
+              uint64_t scratch_bytes) {
+    const uint32_t rec_bytes = kind == RT_ACCEL_KIND_BLAS ? 48u : 80u;
+    const uint64_t need_accel = accel_bytes_for(n, rec_bytes, kind == RT_ACCEL_KIND_BLAS ? n_geoms + 1u : 0u);
+    const RefitLayout L = refit_layout(n);
+    if (accel_bytes < need_accel) return set_error(ctx, RT_ERR_OOM, "accel buffer smaller than its build size");
+    if (scratch_bytes < L.total) return set_error(ctx, RT_ERR_OOM, "scratch smaller than rt_get_refit_scratch_bytes");
+    if (reinterpret_cast<uintptr_t>(accel) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "accel must be 256-byte aligned");
+    if (reinterpret_cast<uintptr_t>(scratch) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "scratch must be 256-byte aligned");
+    if (n == 0) return RT_OK;  // an empty structure has nothing to refit
+    uint8_t *A = static_cast<uint8_t *>(accel);
+    uint8_t *S = static_cast<uint8_t *>(scratch);
+    const uint32_t cap = node_capacity_for(n);
+    rt_accel_header *hdr = reinterpret_cast<rt_accel_header *>(A);
+    uint4 *nodes = reinterpret_cast<uint4 *>(A + RT_ACCEL_HEADER_BYTES);
+    uint4 *recs = reinterpret_cast<uint4 *>(A + RT_ACCEL_HEADER_BYTES + (uint64_t)cap * 80u);
+    uint32_t *flag = reinterpret_cast<uint32_t *>(S + L.flag);
+    float *leaf_box = reinterpret_cast<float *>(S + L.leaf_box);
+    float *node_box = reinterpret_cast<float *>(S + L.node_box);
+    uint32_t *parent = reinterpret_cast<uint32_t *>(S + L.parent);
+    uint32_t *arrive = reinterpret_cast<uint32_t *>(S + L.arrive);
+    uint32_t *hdr_status = reinterpret_cast<uint32_t *>(A) + 7;  // rt_accel_header::status
+    k_refit_begin<<<1, 32, 0, st>>>(hdr, kind, n, n_geoms, cap, flag, ctx->d_err);
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(parent, 0xff, (size_t)cap * 4u, st));
+    const unsigned nbc = (cap + 255u) / 256u, nbn = (n + 255u) / 256u;
+    k_refit_links<<<nbc, 256, 0, st>>>(nodes, hdr, cap, flag, parent, arrive, ctx->d_err);
+    if (kind == RT_ACCEL_KIND_BLAS)
+        k_refit_tris<<<nbn, 256, 0, st>>>(*gp, n, recs, leaf_box, flag, ctx->d_err, hdr_status);
+    else
+        k_refit_inst<<<nbn, 256, 0, st>>>(instances, n, recs, leaf_box, flag, ctx->d_err);
+    k_refit_nodes<<<nbc, 256, 0, st>>>(nodes, hdr, cap, n, leaf_box, node_box, parent, arrive, flag, ctx->d_err);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+// Fills the geometry table of a bottom-level input; RT_OK or an error.
+int geom_params(rt_context *ctx, const rt_geometry_triangles *geoms, uint32_t n_geoms, GeomParams &gp,
+                uint64_t &total, const char *who) {
+    std::memset(&gp, 0, sizeof(gp));
+    gp.n_geoms = n_geoms;
+    total = 0;
+    for (uint32_t g = 0; g < n_geoms; ++g) {
+        const rt_geometry_triangles &G = geoms[g];
+        if (G.tri_count && (!G.vertices || G.vertex_stride < 12u ||
+                            (G.index_type != RT_INDEX_UINT32 && G.index_type != RT_INDEX_NONE) ||
+                            (G.index_type == RT_INDEX_UINT32 && !G.indices)))
+            return set_error(ctx, RT_ERR_INVALID_ARG, who);
+        if (G.index_type == RT_INDEX_NONE && G.tri_count && (uint64_t)G.tri_count * 3u - 1u > G.max_vertex)
+            return set_error(ctx, RT_ERR_INVALID_ARG, who);
+        gp.table[g] = (uint32_t)total;
+        gp.g[g] = G;
+        total += G.tri_count;
+    }
+    if (total > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 2^30-1 triangles");
+    gp.table[n_geoms] = (uint32_t)total;
+    return RT_OK;
+}
+
 }  // namespace
 }  // namespace rtc
 
@@ -917,23 +1168,9 @@ extern "C" rt_status rt_build_blas(rt_context *ctx, rt_stream stream, const rt_g
     if ((flags & RT_BUILD_MORTON30) && (flags & RT_BUILD_MORTON63))
         return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_MORTON30 and RT_BUILD_MORTON63 are exclusive");
     static thread_local GeomParams gp;
-    std::memset(&gp, 0, sizeof(gp));
-    gp.n_geoms = n_geoms;
     uint64_t total = 0;
-    for (uint32_t g = 0; g < n_geoms; ++g) {
-        const rt_geometry_triangles &G = geoms[g];
-        if (G.tri_count && (!G.vertices || G.vertex_stride < 12u ||
-                            (G.index_type != RT_INDEX_UINT32 && G.index_type != RT_INDEX_NONE) ||
-                            (G.index_type == RT_INDEX_UINT32 && !G.indices)))
-            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas: bad geometry descriptor");
-        if (G.index_type == RT_INDEX_NONE && G.tri_count && (uint64_t)G.tri_count * 3u - 1u > G.max_vertex)
-            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas: non-indexed geometry exceeds max_vertex");
-        gp.table[g] = (uint32_t)total;
-        gp.g[g] = G;
-        total += G.tri_count;
-    }
-    if (total > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 2^30-1 triangles");
-    gp.table[n_geoms] = (uint32_t)total;
+    int rc = geom_params(ctx, geoms, n_geoms, gp, total, "rt_build_blas: bad geometry descriptor");
+    if (rc) return rc;
     BuildCall bc{RT_ACCEL_KIND_BLAS, (uint32_t)total, 48u, n_geoms, flags};
     return run_build(ctx, static_cast<cudaStream_t>(stream), bc, &gp, nullptr, accel, accel_bytes, scratch,
                      scratch_bytes, nullptr);
@@ -949,6 +1186,36 @@ extern "C" rt_status rt_build_tlas(rt_context *ctx, rt_stream stream, const rt_i
     BuildCall bc{RT_ACCEL_KIND_TLAS, n, 80u, 0u, flags};
     return run_build(ctx, static_cast<cudaStream_t>(stream), bc, nullptr, instances, accel, accel_bytes, scratch,
                      scratch_bytes, nullptr);
+}
+
+extern "C" rt_status rt_get_refit_scratch_bytes(uint32_t prim_count, uint64_t *bytes) {
+    if (!bytes) return RT_ERR_INVALID_ARG;
+    if (prim_count > (1u << 30) - 1u) return RT_ERR_UNSUPPORTED;
+    *bytes = refit_layout(prim_count).total;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_refit_blas(rt_context *ctx, rt_stream stream, const rt_geometry_triangles *geoms,
+                                   uint32_t n_geoms, void *accel, uint64_t accel_bytes, void *scratch,
+                                   uint64_t scratch_bytes) {
+    if (!ctx || !accel || !scratch || (n_geoms && !geoms))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_refit_blas: null argument");
+    if (n_geoms > (uint32_t)kMaxGeoms) return set_error(ctx, RT_ERR_UNSUPPORTED, "more than 256 geometries in one BLAS");
+    static thread_local GeomParams gp;
+    uint64_t total = 0;
+    int rc = geom_params(ctx, geoms, n_geoms, gp, total, "rt_refit_blas: bad geometry descriptor");
+    if (rc) return rc;
+    return run_refit(ctx, static_cast<cudaStream_t>(stream), RT_ACCEL_KIND_BLAS, (uint32_t)total, n_geoms, &gp,
+                     nullptr, accel, accel_bytes, scratch, scratch_bytes);
+}
+
+extern "C" rt_status rt_refit_tlas(rt_context *ctx, rt_stream stream, const rt_instance *instances, uint32_t n,
+                                   void *accel, uint64_t accel_bytes, void *scratch, uint64_t scratch_bytes) {
+    if (!ctx || !accel || !scratch || (n && !instances))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_refit_tlas: null argument");
+    if (n > (1u << 30) - 1u) return set_error(ctx, RT_ERR_UNSUPPORTED, "too many instances");
+    return run_refit(ctx, static_cast<cudaStream_t>(stream), RT_ACCEL_KIND_TLAS, n, 0u, nullptr, instances, accel,
+                     accel_bytes, scratch, scratch_bytes);
 }
 
 extern "C" uint64_t rt_accel_address(const void *accel) { return (uint64_t)(uintptr_t)accel; }

@@ -23,7 +23,9 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/rtcore_cache.h"
@@ -770,6 +772,80 @@ extern "C" rt_status rt_cache_set_params(rt_context *ctx, rt_stream stream, void
     RT_CUDA_CTX(ctx, cudaMemcpyAsync(S->params, params, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
     k_cache_refresh_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(S);
     RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoints
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct CheckpointHeader {
+    char magic[4];         // "RTMC"
+    uint32_t version;      // 1
+    uint32_t params;       // kParams
+    uint32_t reserved0;
+    uint64_t state_bytes;  // sizeof(CacheState)
+    uint64_t checksum;     // FNV-1a 64 of the state bytes
+    uint8_t reserved[32];
+};
+static_assert(sizeof(CheckpointHeader) == 64, "checkpoint header");
+
+uint64_t fnv1a64(const uint8_t *p, size_t n) {
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_cache_save(rt_context *ctx, rt_stream stream, const void *cache, const char *path) {
+    if (!ctx || !cache || !path) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_save: null argument");
+    std::vector<uint8_t> state(sizeof(CacheState));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(state.data(), cache, state.size(), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
+    CheckpointHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, "RTMC", 4);
+    h.version = 1u;
+    h.params = (uint32_t)kParams;
+    h.state_bytes = state.size();
+    h.checksum = fnv1a64(state.data(), state.size());
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_save: cannot open the file for writing");
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(state.data(), 1, state.size(), f) == state.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_save: write failed");
+    }
+    return RT_OK;
+}
+
+extern "C" rt_status rt_cache_load(rt_context *ctx, rt_stream stream, void *cache, const char *path) {
+    if (!ctx || !cache || !path) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_load: null argument");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_load: cannot open the file");
+    CheckpointHeader h;
+    std::vector<uint8_t> state(sizeof(CacheState));
+    const bool got = std::fread(&h, sizeof(h), 1, f) == 1 &&
+                     std::memcmp(h.magic, "RTMC", 4) == 0 && h.version == 1u && h.params == (uint32_t)kParams &&
+                     h.state_bytes == state.size() && std::fread(state.data(), 1, state.size(), f) == state.size();
+    const bool at_end = got && std::fgetc(f) == EOF;
+    std::fclose(f);
+    if (!got || !at_end)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_load: not a cache checkpoint of this network");
+    if (fnv1a64(state.data(), state.size()) != h.checksum)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_load: checksum mismatch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RT_CUDA_CTX(ctx, cudaMemcpyAsync(cache, state.data(), state.size(), cudaMemcpyHostToDevice, st));
+    RT_CUDA_CTX(ctx, cudaStreamSynchronize(st));
     return RT_OK;
 }
 

@@ -175,6 +175,9 @@ PROTOTYPES = {
     "rt_build_blas": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _u32, _vp, _u64, _vp, _u64]),
     "rt_build_tlas": (_i32, [_vp, _vp, _vp, _u32, _u32, _vp, _u64, _vp, _u64]),
     "rt_build_blas_static_scratch": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _u32, _vp, _u64]),
+    "rt_get_refit_scratch_bytes": (_i32, [_u32, C.POINTER(_u64)]),
+    "rt_refit_blas": (_i32, [_vp, _vp, C.POINTER(GeometryTriangles), _u32, _vp, _u64, _vp, _u64]),
+    "rt_refit_tlas": (_i32, [_vp, _vp, _vp, _u32, _vp, _u64, _vp, _u64]),
     "rt_accel_address": (_u64, [_vp]),
     "rt_accel_info": (_i32, [_vp, _vp, _vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "rt_trace_rays": (_i32, [_vp, _vp, C.POINTER(Pipeline), C.POINTER(Sbt), _u64, C.POINTER(Camera), _vp,
@@ -222,11 +225,15 @@ PROTOTYPES = {
     "rt_cache_gradient": (_i32, [_vp, _vp, _vp, _vp, _vp, _u32, _vp]),
     "rt_cache_get_params": (_i32, [_vp, _vp, _vp, _vp]),
     "rt_cache_set_params": (_i32, [_vp, _vp, _vp, _vp]),
+    "rt_cache_save": (_i32, [_vp, _vp, _vp, C.c_char_p]),
+    "rt_cache_load": (_i32, [_vp, _vp, _vp, C.c_char_p]),
     # seeded scenes declared in include/rtcore_scene.h (host code)
     "rt_scene_soup": (_i32, [_u64, _u32, _vp, _vp]),
     "rt_scene_box_counts": (_i32, [_u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "rt_scene_box": (_i32, [_u64, _u32, _u32, _vp, _vp, _vp, _vp]),
     "rt_scene_incoherent_rays": (_i32, [_u64, _u32, _vp, _vp, _f, _vp]),
+    "rt_obj_counts": (_i32, [C.c_char_p, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "rt_obj_load": (_i32, [C.c_char_p, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -332,6 +339,15 @@ class Context:
     def build_tlas(self, instances, n, flags, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
         self.check(self.lib.rt_build_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, flags, _ptr(accel),
                                           accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_tlas")
+
+    def refit_blas(self, geoms, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
+        arr = (GeometryTriangles * max(1, len(geoms)))(*geoms)
+        self.check(self.lib.rt_refit_blas(self.h, _stream_ptr(stream), arr, len(geoms), _ptr(accel), accel_bytes,
+                                          _ptr(scratch), scratch_bytes), "rt_refit_blas")
+
+    def refit_tlas(self, instances, n, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
+        self.check(self.lib.rt_refit_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, _ptr(accel), accel_bytes,
+                                          _ptr(scratch), scratch_bytes), "rt_refit_tlas")
 
     def accel_info(self, accel, stream=None):
         nc, pc, d = C.c_uint32(), C.c_uint32(), C.c_uint32()
@@ -472,6 +488,14 @@ class Context:
         self.check(self.lib.rt_cache_set_params(self.h, _stream_ptr(stream), _ptr(cache), _ptr(params)),
                    "rt_cache_set_params")
 
+    def cache_save(self, cache, path, stream=None) -> None:
+        self.check(self.lib.rt_cache_save(self.h, _stream_ptr(stream), _ptr(cache), os.fsencode(str(path))),
+                   "rt_cache_save")
+
+    def cache_load(self, cache, path, stream=None) -> None:
+        self.check(self.lib.rt_cache_load(self.h, _stream_ptr(stream), _ptr(cache), os.fsencode(str(path))),
+                   "rt_cache_load")
+
     # ---- utilities
     def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:
         self.check(self.lib.rt_sort_pairs(self.h, _stream_ptr(stream), _ptr(keys), _ptr(vals), n, key_bits,
@@ -538,6 +562,14 @@ def tuning_cache_store(path, key: str, t: BatchTuning, ms: float) -> None:
     rc = load().rt_batch_tuning_cache_store(os.fsencode(str(path)), key.encode(), C.byref(t), ms)
     if rc != RT_OK:
         raise RtError(rc, "rt_batch_tuning_cache_store")
+
+
+def refit_scratch_bytes(prim_count: int) -> int:
+    out = C.c_uint64()
+    rc = load().rt_get_refit_scratch_bytes(prim_count, C.byref(out))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_get_refit_scratch_bytes")
+    return out.value
 
 
 def sort_scratch_bytes(n: int, key_bits: int) -> int:

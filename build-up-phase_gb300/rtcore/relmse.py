@@ -7,12 +7,15 @@ path tracer, both measured against a converged plain reference.
 relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Both
 forms run one sample per call; the time of a call is its CUDA-event duration
 (training included for the learned form), image read-backs are not timed.
-The curve is sampled at doubling sample counts and at the end of the budget.
+The curve is sampled at sample counts growing by 1.25x and at the end of the
+budget; the time to a target relMSE is interpolated log-log between the two
+samples around the crossing.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import time
 
 import numpy as np
@@ -79,7 +82,7 @@ def _checkpoints(n: int):
     k = 1
     while k <= n:
         yield k
-        k *= 2
+        k = max(k + 1, int(math.ceil(k * 1.25)))
 
 
 def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, cached: bool,
@@ -119,10 +122,18 @@ def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: f
 
 
 def time_to(curve, target: float):
-    """First elapsed time at which relMSE <= target (None if never)."""
+    """Elapsed time at which relMSE first reaches target, interpolated
+    log-log between the samples around the crossing (None if never)."""
+    prev = None
     for ms, s, r in curve:
         if r <= target:
-            return ms
+            if prev is None or prev[2] <= r or prev[0] <= 0.0:
+                return ms
+            lt0, lt1 = math.log(prev[0]), math.log(ms)
+            lr0, lr1 = math.log(prev[2]), math.log(r)
+            f = (math.log(target) - lr0) / (lr1 - lr0)
+            return round(math.exp(lt0 + f * (lt1 - lt0)), 3)
+        prev = (ms, s, r)
     return None
 
 
@@ -156,6 +167,8 @@ def main(argv=None) -> int:
            "relmse_at_budget": {"plain": plain[-1][2], "cached": cached[-1][2]},
            "time_to_target_ms": {"target": a.target, "plain": time_to(plain, a.target),
                                  "cached": time_to(cached, a.target)}}
+    tp, tc = res["time_to_target_ms"]["plain"], res["time_to_target_ms"]["cached"]
+    res["time_ratio_cached_over_plain"] = round(tc / tp, 3) if tp and tc else None
     js = json.dumps(res)
     print(js)
     if a.out:

@@ -60,6 +60,39 @@ def box(seed: int, n_spheres: int, freq: int):
     return v, i, tm, m
 
 
+def load_obj(path):
+    """(vertices float32 [n, 3], indices uint32 [m, 3], tri_material uint32 [m],
+    number of materials) of a Wavefront OBJ file (rt_obj_load)."""
+    import os
+    lib = load()
+    b = os.fsencode(str(path))
+    nv, nt, nm = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    rc = lib.rt_obj_counts(b, C.byref(nv), C.byref(nt), C.byref(nm))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_obj_counts")
+    v = np.empty((nv.value, 3), np.float32)
+    i = np.empty((nt.value, 3), np.uint32)
+    tm = np.empty(nt.value, np.uint32)
+    rc = lib.rt_obj_load(b, _ptr(v), _ptr(i), _ptr(tm))
+    if rc != RT_OK:
+        raise RtError(rc, "rt_obj_load")
+    return v, i, tm, nm.value
+
+
+def write_obj(path, v: np.ndarray, i: np.ndarray, tri_material: np.ndarray | None = None) -> None:
+    """Writes vertices and triangles as OBJ text (floats with 9 significant
+    digits, which read back to the same float32)."""
+    lines = [f"v {a:.9g} {b:.9g} {c:.9g}" for a, b, c in np.asarray(v, np.float32).tolist()]
+    cur = None
+    for k, (a, b, c) in enumerate((np.asarray(i, np.int64) + 1).tolist()):
+        if tri_material is not None and tri_material[k] != cur:
+            cur = int(tri_material[k])
+            lines.append(f"usemtl m{cur}")
+        lines.append(f"f {a} {b} {c}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def incoherent_rays(seed: int, n: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), tmax: float = 1e30):
     rays = np.empty(n, RAY_DTYPE)
     lo_a = np.asarray(lo, np.float32)

@@ -274,6 +274,25 @@ rt_status rt_build_tlas(rt_context *ctx, rt_stream stream,
                         uint32_t flags, void *accel, uint64_t accel_bytes,
                         void *scratch, uint64_t scratch_bytes);
 
+/*
+ * Refit: the update mode of a build (VK_BUILD_ACCELERATION_STRUCTURE_MODE_UPDATE_KHR;
+ * the sample builds once, main.cpp:808, :932).  Takes the inputs of the build
+ * that made `accel` with new vertex positions or geometry transforms (BLAS:
+ * same geometry and triangle counts) or new instance transforms and
+ * references (TLAS: same instance count), recomputes every leaf record and
+ * box and keeps the tree.  For animation whose motion keeps the tree
+ * reasonable; rebuild when it degrades.  A BLAS refit moves its bounds, so the
+ * TLASes that reference it need a refit or a rebuild after it.  A structure
+ * that does not match the inputs is left unchanged and RT_ERR_INVALID_ARG
+ * surfaces at rt_sync.  scratch: rt_get_refit_scratch_bytes(primitives),
+ * about 56 bytes per primitive.
+ */
+rt_status rt_get_refit_scratch_bytes(uint32_t prim_count, uint64_t *bytes);
+rt_status rt_refit_blas(rt_context *ctx, rt_stream stream, const rt_geometry_triangles *geoms, uint32_t n_geoms,
+                        void *accel, uint64_t accel_bytes, void *scratch, uint64_t scratch_bytes);
+rt_status rt_refit_tlas(rt_context *ctx, rt_stream stream, const rt_instance *instances, uint32_t n,
+                        void *accel, uint64_t accel_bytes, void *scratch, uint64_t scratch_bytes);
+
 /* vkGetAccelerationStructureDeviceAddressKHR (main.cpp:665-672): the handle
  * by which instances and trace calls name a built structure. */
 uint64_t rt_accel_address(const void *accel);

@@ -79,6 +79,15 @@ rt_status rt_cache_gradient(rt_context *ctx, rt_stream stream, void *cache, cons
 rt_status rt_cache_get_params(rt_context *ctx, rt_stream stream, const void *cache, float *params);
 rt_status rt_cache_set_params(rt_context *ctx, rt_stream stream, void *cache, const float *params);
 
+/* Checkpoint: the whole state (FP32 weights, Adam moments and step, the
+ * encoding box, the optimiser constants) to / from a file: a 64-byte header
+ * ("RTMC", format version, parameter count, state bytes, FNV-1a 64 checksum of
+ * the state) and the state bytes.  Load rejects a file of another format,
+ * size or checksum with RT_ERR_INVALID_ARG and leaves the cache unchanged.
+ * Both synchronise `stream`. */
+rt_status rt_cache_save(rt_context *ctx, rt_stream stream, const void *cache, const char *path);
+rt_status rt_cache_load(rt_context *ctx, rt_stream stream, void *cache, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,20 @@ rt_status rt_scene_box(uint64_t seed, uint32_t n_spheres, uint32_t freq, float *
 rt_status rt_scene_incoherent_rays(uint64_t seed, uint32_t n, const float lo[3], const float hi[3], float tmax,
                                    rt_ray *rays);
 
+/* Wavefront OBJ mesh (host files): counts first, then the arrays.
+ * `v x y z` vertices (further numbers on the line ignored); `f` faces of three
+ * or more references a, a/t, a//n or a/t/n (1-based, negative = relative to
+ * the vertices read so far) split into the fan (a0, ai, ai+1); `usemtl name`
+ * selects the material of the following faces, numbered 0, 1, ... in the order
+ * faces first use them (faces before any usemtl use an unnamed material);
+ * every other statement is skipped.  vertices: 3 floats per vertex; indices:
+ * 3 per triangle; tri_material (nullable): one per triangle.  A missing file,
+ * a malformed number or a reference outside the vertices gives
+ * RT_ERR_INVALID_ARG.  No counterpart in the reference, which hard-codes its
+ * arrays (vulkan-raytraced-triangle/main.cpp:676-682). */
+rt_status rt_obj_counts(const char *path, uint32_t *n_vertices, uint32_t *n_tris, uint32_t *n_materials);
+rt_status rt_obj_load(const char *path, float *vertices, uint32_t *indices, uint32_t *tri_material);
+
 #ifdef __cplusplus
 }
 #endif

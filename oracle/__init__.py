@@ -53,6 +53,8 @@ def load() -> C.CDLL:
         "orc_tlas_accel_bytes": (u64, [u32]),
         "orc_build_blas": (i32, [vp, u32, u32, vp, u64, vp]),
         "orc_build_tlas": (i32, [vp, u32, u32, vp, u64]),
+        "orc_refit_blas": (i32, [vp, u32, vp]),
+        "orc_refit_tlas": (i32, [vp, u32, vp]),
         "orc_trace_closest": (None, [vp, vp, vp, vp, u32, u32, vp]),
         "orc_trace_any": (None, [vp, vp, vp, u32, u32, vp]),
         "orc_brute_closest": (None, [vp, u32, vp, vp, u32, i32, u32]),
@@ -165,6 +167,17 @@ def build_tlas(instances: np.ndarray, flags: int = 0):
     buf = _aligned_zeros(nbytes)
     rc = lib.orc_build_tlas(instances.ctypes.data, len(instances), flags, buf.ctypes.data, nbytes)
     return buf, rc
+
+
+def refit_blas(accel: np.ndarray, items) -> int:
+    """rt_refit_blas on the CPU, in place on an oracle BLAS buffer."""
+    hg = HostGeoms(items)
+    return load().orc_refit_blas(hg.arr, hg.n, accel.ctypes.data)
+
+
+def refit_tlas(accel: np.ndarray, instances: np.ndarray) -> int:
+    instances = np.ascontiguousarray(instances, INSTANCE_DTYPE)
+    return load().orc_refit_tlas(instances.ctypes.data, len(instances), accel.ctypes.data)
 
 
 def _aligned_zeros(nbytes: int) -> np.ndarray:

@@ -860,6 +860,85 @@ int prep_triangles(const orc_geometry *geoms, uint32_t n_geoms, BuildInput &in, 
     return status;
 }
 
+/* Leaf record and world box of instance i. */
+void inst_input(const rt_instance &I, uint32_t i, rt_inst_record &rec, Box &b) {
+    std::memset(&rec, 0, sizeof(rec));
+    bool ok = invert3x4(I.transform, rec.world_to_object);
+    rec.accel_ref = I.accel_ref;
+    rec.custom_index_and_mask = I.custom_index_and_mask;
+    rec.sbt_offset_and_flags = I.sbt_offset_and_flags;
+    rec.instance_id = i;
+    const rt_accel_header *bh = (const rt_accel_header *)(uintptr_t)I.accel_ref;
+    b = box_empty();
+    if (ok && bh && bh->prim_count > 0) {
+        for (int c = 0; c < 8; ++c) {
+            float pt[3] = {(c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
+                           (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
+                           (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]};
+            float w[3];
+            xform_point(I.transform, pt, w);
+            for (int a = 0; a < 3; ++a) { b.lo[a] = fmn(b.lo[a], w[a]); b.hi[a] = fmx(b.hi[a], w[a]); }
+        }
+    }
+}
+
+/* Refit of the nodes of `accel` whose leaf records already hold the new
+ * primitives, leaf_box[r] the box of record r: nodes in reverse order (every
+ * child follows its parent), each node's box the union of its slots'. */
+void refit_nodes(uint8_t *base, const std::vector<Box> &leaf_box) {
+    rt_accel_header *h = (rt_accel_header *)base;
+    rt_bvh8_node *nodes = (rt_bvh8_node *)(base + h->node_offset);
+    std::vector<Box> nb(h->node_count);
+    for (int64_t k = (int64_t)h->node_count - 1; k >= 0; --k) {
+        rt_bvh8_node &nd = nodes[k];
+        Box sbox[8];
+        bool used[8];
+        Box node = box_empty();
+        for (int s = 0; s < 8; ++s) {
+            const uint8_t meta = nd.meta[s];
+            used[s] = meta != 0;
+            sbox[s] = box_empty();
+            if ((nd.imask >> s) & 1u) {
+                sbox[s] = nb[nd.child_base + (uint32_t)__builtin_popcount(nd.imask & ((1u << s) - 1u))];
+            } else if (meta) {
+                const uint32_t cnt = (uint32_t)__builtin_popcount(meta >> 5), first = nd.prim_base + (meta & 0x1fu);
+                for (uint32_t j = 0; j < cnt; ++j) sbox[s] = box_union(sbox[s], leaf_box[first + j]);
+            }
+            if (used[s]) node = box_union(node, sbox[s]);
+        }
+        const uint32_t cb = nd.child_base, pb = nd.prim_base;
+        const uint8_t imask = nd.imask;
+        uint8_t meta[8];
+        std::memcpy(meta, nd.meta, 8);
+        write_node(nd, node, sbox, used);
+        nd.child_base = cb;
+        nd.prim_base = pb;
+        nd.imask = imask;
+        std::memcpy(nd.meta, meta, 8);
+        nb[k] = node;
+    }
+    for (int a = 0; a < 3; ++a) { h->bounds_lo[a] = nb[0].lo[a]; h->bounds_hi[a] = nb[0].hi[a]; }
+}
+
+/* The tree of `accel` is consistent: children after their parent, leaf
+ * ranges inside the records. */
+bool tree_ok(const uint8_t *base) {
+    const rt_accel_header *h = (const rt_accel_header *)base;
+    if (h->node_count == 0 || h->node_count > h->node_capacity) return false;
+    const rt_bvh8_node *nodes = (const rt_bvh8_node *)(base + h->node_offset);
+    for (uint32_t k = 0; k < h->node_count; ++k) {
+        const rt_bvh8_node &nd = nodes[k];
+        const uint32_t ni = (uint32_t)__builtin_popcount(nd.imask);
+        if (ni && (nd.child_base <= k || (uint64_t)nd.child_base + ni > h->node_count)) return false;
+        for (int s = 0; s < 8; ++s)
+            if (!((nd.imask >> s) & 1u) && nd.meta[s]) {
+                const uint32_t cnt = (uint32_t)__builtin_popcount(nd.meta[s] >> 5);
+                if ((uint64_t)nd.prim_base + (nd.meta[s] & 0x1fu) + cnt > h->prim_count) return false;
+            }
+    }
+    return true;
+}
+
 }  // namespace
 
 /* ====================================================================== */
@@ -907,26 +986,9 @@ int orc_build_tlas(const rt_instance *instances, uint32_t n, uint32_t flags, voi
     in.active.resize(n);
     in.records.assign((size_t)n * 80u, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const rt_instance &I = instances[i];
         rt_inst_record rec;
-        std::memset(&rec, 0, sizeof(rec));
-        bool ok = invert3x4(I.transform, rec.world_to_object);
-        rec.accel_ref = I.accel_ref;
-        rec.custom_index_and_mask = I.custom_index_and_mask;
-        rec.sbt_offset_and_flags = I.sbt_offset_and_flags;
-        rec.instance_id = i;
-        const rt_accel_header *bh = (const rt_accel_header *)(uintptr_t)I.accel_ref;
-        Box b = box_empty();
-        if (ok && bh && bh->prim_count > 0) {
-            for (int c = 0; c < 8; ++c) {
-                float pt[3] = {(c & 1) ? bh->bounds_hi[0] : bh->bounds_lo[0],
-                               (c & 2) ? bh->bounds_hi[1] : bh->bounds_lo[1],
-                               (c & 4) ? bh->bounds_hi[2] : bh->bounds_lo[2]};
-                float w[3];
-                xform_point(I.transform, pt, w);
-                for (int a = 0; a < 3; ++a) { b.lo[a] = fmn(b.lo[a], w[a]); b.hi[a] = fmx(b.hi[a], w[a]); }
-            }
-        }
+        Box b;
+        inst_input(instances[i], i, rec, b);
         in.boxes[i] = b;
         in.active[i] = box_is_empty(b) ? 0 : 1;
         std::memcpy(&in.records[(size_t)i * 80u], &rec, 80);
@@ -934,6 +996,56 @@ int orc_build_tlas(const rt_instance *instances, uint32_t n, uint32_t flags, voi
     BuildResult r = build_wide(in, flags, nullptr);
     std::vector<uint32_t> none;
     write_accel(accel, RT_ACCEL_KIND_TLAS, n, 0, flags, node_capacity_for(n), need, r, 80, none);
+    return 0;
+}
+
+int orc_refit_blas(const orc_geometry *geoms, uint32_t n_geoms, void *accel) {
+    uint8_t *base = (uint8_t *)accel;
+    rt_accel_header *h = (rt_accel_header *)base;
+    uint64_t n = 0;
+    for (uint32_t g = 0; g < n_geoms; ++g) n += geoms[g].tri_count;
+    if (h->magic != RT_ACCEL_MAGIC || h->kind != RT_ACCEL_KIND_BLAS || h->prim_count != n ||
+        h->geom_count != n_geoms || h->node_capacity != node_capacity_for((uint32_t)n))
+        return RT_ERR_INVALID_ARG;
+    if (n == 0) return 0;
+    if (!tree_ok(base)) return RT_ERR_INVALID_ARG;
+    BuildInput in;
+    std::vector<uint32_t> gtab;
+    const int st = prep_triangles(geoms, n_geoms, in, gtab);
+    std::vector<Box> leaf_box(n);
+    uint8_t *recs = base + h->prim_offset;
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t ids[3];
+        for (int k = 0; k < 3; ++k) std::memcpy(&ids[k], recs + (size_t)r * 48u + 16u * k + 12u, 4);
+        const uint32_t gi = ids[0], g = ids[1], p = ids[2];
+        if (g >= n_geoms || p >= geoms[g].tri_count || gi != gtab[g] + p) return RT_ERR_INVALID_ARG;
+        std::memcpy(recs + (size_t)r * 48u, &in.records[(size_t)gi * 48u], 48);
+        leaf_box[r] = in.boxes[gi];
+    }
+    refit_nodes(base, leaf_box);
+    if (st && h->status == 0) h->status = (uint32_t)(-st);
+    return st;
+}
+
+int orc_refit_tlas(const rt_instance *instances, uint32_t n, void *accel) {
+    uint8_t *base = (uint8_t *)accel;
+    rt_accel_header *h = (rt_accel_header *)base;
+    if (h->magic != RT_ACCEL_MAGIC || h->kind != RT_ACCEL_KIND_TLAS || h->prim_count != n ||
+        h->node_capacity != node_capacity_for(n))
+        return RT_ERR_INVALID_ARG;
+    if (n == 0) return 0;
+    if (!tree_ok(base)) return RT_ERR_INVALID_ARG;
+    std::vector<Box> leaf_box(n);
+    uint8_t *recs = base + h->prim_offset;
+    for (uint32_t r = 0; r < n; ++r) {
+        rt_inst_record rec;
+        std::memcpy(&rec, recs + (size_t)r * 80u, 80);
+        const uint32_t i = rec.instance_id;
+        if (i >= n) return RT_ERR_INVALID_ARG;
+        inst_input(instances[i], i, rec, leaf_box[r]);
+        std::memcpy(recs + (size_t)r * 80u, &rec, 80);
+    }
+    refit_nodes(base, leaf_box);
     return 0;
 }
 

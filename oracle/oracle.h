@@ -57,6 +57,14 @@ int orc_build_blas(const orc_geometry *geoms, uint32_t n_geoms, uint32_t flags,
 int orc_build_tlas(const rt_instance *instances, uint32_t n, uint32_t flags,
                    void *accel, uint64_t accel_bytes);
 
+/* Refit restatement (rt_refit_blas / rt_refit_tlas): recomputes the leaf
+ * records and every box of `accel` from new inputs in the existing tree,
+ * nodes in reverse breadth-first order.  Returns 0, RT_ERR_INVALID_ARG when
+ * the structure does not match the inputs (left unchanged), or the build's
+ * RT_ERR_BOUNDS status for an index beyond max_vertex. */
+int orc_refit_blas(const orc_geometry *geoms, uint32_t n_geoms, void *accel);
+int orc_refit_tlas(const rt_instance *instances, uint32_t n, void *accel);
+
 /* Closest-hit / any-hit traversal of the BVH8 in `accel` (host memory),
  * mirroring the GPU kernel's visiting order.  stats (nullable) receives
  * [nodes visited, triangles tested] summed over rays.  n_threads 0 = all. */

@@ -91,20 +91,43 @@ class GpuBlas:
     """A BLAS built through rt_get_blas_build_sizes + rt_build_blas."""
 
     def __init__(self, ctx, items, flags: int = 0, stream=None):
-        import rtcore
         import torch
         self.keep = []
+        geoms = self._geoms(items, self.keep)
+        self.sizes = ctx.blas_sizes([g.tri_count for g in geoms], flags)
+        self.accel = torch.empty(self.sizes.accel_bytes, dtype=torch.uint8, device="cuda")
+        self.scratch = torch.empty(self.sizes.scratch_bytes, dtype=torch.uint8, device="cuda")
+        ctx.build_blas(geoms, flags, self.accel, self.sizes.accel_bytes, self.scratch, self.sizes.scratch_bytes,
+                       stream)
+        ctx.sync(stream)
+        self.addr = ctx.address(self.accel)
+
+    def refit(self, ctx, items, stream=None) -> None:
+        """rt_refit_blas with new (vertices, indices, transform) items."""
+        import rtcore
+        import torch
+        keep = []
+        geoms = self._geoms(items, keep)
+        n = sum(g.tri_count for g in geoms)
+        nb = rtcore.refit_scratch_bytes(n)
+        scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        ctx.refit_blas(geoms, self.accel, self.sizes.accel_bytes, scratch, nb, stream)
+        ctx.sync(stream)
+
+    @staticmethod
+    def _geoms(items, keep):
+        import rtcore
         geoms = []
         for v, i, xf in items:
             g = rtcore.GeometryTriangles()
             dv = dev(np.ascontiguousarray(v, np.float32))
-            self.keep.append(dv)
+            keep.append(dv)
             g.vertices = dv.data_ptr()
             g.vertex_stride = 12
             g.max_vertex = max(0, len(v) - 1)
             if i is not None:
                 di = dev(np.ascontiguousarray(i, np.uint32))
-                self.keep.append(di)
+                keep.append(di)
                 g.index_type = rtcore.RT_INDEX_UINT32
                 g.indices = di.data_ptr()
                 g.tri_count = len(i)
@@ -114,16 +137,10 @@ class GpuBlas:
             g.flags = rtcore.RT_GEOMETRY_OPAQUE
             if xf is not None:
                 dx = dev(np.ascontiguousarray(xf, np.float32))
-                self.keep.append(dx)
+                keep.append(dx)
                 g.transform = dx.data_ptr()
             geoms.append(g)
-        self.sizes = ctx.blas_sizes([g.tri_count for g in geoms], flags)
-        self.accel = torch.empty(self.sizes.accel_bytes, dtype=torch.uint8, device="cuda")
-        self.scratch = torch.empty(self.sizes.scratch_bytes, dtype=torch.uint8, device="cuda")
-        ctx.build_blas(geoms, flags, self.accel, self.sizes.accel_bytes, self.scratch, self.sizes.scratch_bytes,
-                       stream)
-        ctx.sync(stream)
-        self.addr = ctx.address(self.accel)
+        return geoms
 
     def bytes(self) -> np.ndarray:
         return host(self.accel)
@@ -140,6 +157,15 @@ class GpuTlas:
                        self.sizes.scratch_bytes)
         ctx.sync()
         self.addr = ctx.address(self.accel)
+
+    def refit(self, ctx, instances: np.ndarray) -> None:
+        import rtcore
+        import torch
+        di = dev(instances)
+        nb = rtcore.refit_scratch_bytes(len(instances))
+        scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        ctx.refit_tlas(di, len(instances), self.accel, self.sizes.accel_bytes, scratch, nb)
+        ctx.sync()
 
     def bytes(self) -> np.ndarray:
         return host(self.accel)

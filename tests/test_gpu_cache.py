@@ -169,3 +169,47 @@ def test_params_roundtrip(ctx, cache):
     ctx.cache_set_params(cache, dev(q))
     ctx.sync()
     assert get_params(ctx, cache).tobytes() == q.tobytes()
+
+
+def test_checkpoint_restores_training_state(ctx, cache, tmp_path):
+    """Save after some Adam steps: a fresh cache loaded from the file holds the
+    saved state byte for byte (weights, Adam moments, step count), and the
+    next step from it matches the original's next step (to the rounding of
+    the gradients' atomic accumulation).  Damaged files are rejected without
+    touching the cache."""
+    import rtcore
+    import torch
+    from oracle import mlp
+    x = random_inputs(8192, 21)
+    t = smooth_target(x)
+    dx, dt = dev(x), dev(t)
+    for _ in range(3):
+        ctx.cache_train(cache, dx, dt, len(x), 8192)
+    path = tmp_path / "cache.rtmc"
+    ctx.cache_save(cache, path)
+    ctx.sync()
+    saved = host(cache).copy()
+    other = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device="cuda")
+    ctx.cache_init(other, rtcore.cache_config(seed=99))
+    ctx.cache_load(other, path)
+    ctx.sync()
+    n_state = path.stat().st_size - 64
+    assert host(other)[:n_state].tobytes() == saved[:n_state].tobytes()
+    ctx.cache_train(cache, dx, dt, len(x), 8192)
+    ctx.cache_train(other, dx, dt, len(x), 8192)
+    ctx.sync()
+    a = host(cache)[:4 * mlp.N_PARAMS].view(np.float32)
+    b = host(other)[:4 * mlp.N_PARAMS].view(np.float32)
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
+    step_off = 4 * 4 * mlp.N_PARAMS + 2 * mlp.N_PARAMS
+    assert host(cache)[step_off:step_off + 4].view(np.uint32)[0] == 4
+    assert host(other)[step_off:step_off + 4].view(np.uint32)[0] == 4
+    data = path.read_bytes()
+    before = host(other).copy()
+    for bad in (data[:-1], data + b"x", data[:100] + bytes([data[100] ^ 1]) + data[101:], b"RTMX" + data[4:]):
+        p2 = tmp_path / "bad.rtmc"
+        p2.write_bytes(bad)
+        with pytest.raises(rtcore.RtError) as e:
+            ctx.cache_load(other, p2)
+        assert e.value.code == rtcore.RT_ERR_INVALID_ARG
+    assert host(other).tobytes() == before.tobytes()
