@@ -337,15 +337,27 @@ rt_status cache_store(const char *path, const char *key, const rt_batch_tuning *
     Json *ent = nullptr;
     for (auto &kv : doc.obj)
         if (kv.first == "entries") ent = &kv.second;
-    Json e = tuning_json(*t, ms);
-    if (trials) e.obj.emplace_back("trials", *trials);
-    bool replaced = false;
+    // a new entry, or the tuning fields and time of an existing one updated
+    // in place (its other fields, such as earlier trials, kept)
+    const Json e = tuning_json(*t, ms);
+    Json *old = nullptr;
     for (auto &kv : ent->obj)
-        if (kv.first == key) {
-            kv.second = e;
-            replaced = true;
-        }
-    if (!replaced) ent->obj.emplace_back(key, e);
+        if (kv.first == key && kv.second.kind == Json::Obj) old = &kv.second;
+    if (!old) {
+        ent->obj.emplace_back(key, Json());
+        old = &ent->obj.back().second;
+        old->kind = Json::Obj;
+    }
+    auto put = [&](const std::string &k, const Json &v) {
+        for (auto &kv : old->obj)
+            if (kv.first == k) {
+                kv.second = v;
+                return;
+            }
+        old->obj.emplace_back(k, v);
+    };
+    for (const auto &kv : e.obj) put(kv.first, kv.second);
+    if (trials) put("trials", *trials);
     std::string text;
     write_json(text, doc, 0);
     text.push_back('\n');
@@ -382,6 +394,8 @@ extern "C" rt_status rt_batch_tuning_key(rt_context *ctx, const rt_batch_scene *
         RT_CUDA_CTX(ctx, cudaMemcpy(&prims, src, sizeof(prims), cudaMemcpyDeviceToHost));
         tris += prims;
     }
+    // (the key does not depend on the width the structures were built with:
+    // the width is one of the tuned choices stored under it)
     const int n = std::snprintf(key, key_bytes, "sm%d%d-%d/n2^%u/tris2^%u/px2^%u/d%u", ctx->cc_major, ctx->cc_minor,
                                 ctx->sm_count, log2_bucket(n_scenes), log2_bucket(tris), log2_bucket(pixels),
                                 p->max_depth);
@@ -484,6 +498,16 @@ extern "C" rt_status rt_batch_autotune(rt_context *ctx, const rt_batch_scene *sc
 
     rt_batch_tuning cur;
     rt_batch_default_tuning(&cur);
+    // the width the structures were built with (the first scene with pixels)
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        if (!((uint64_t)scenes[s].width * scenes[s].height) || !scenes[s].scene.accel) continue;
+        uint32_t bf = 0;
+        const void *src = reinterpret_cast<const uint8_t *>(scenes[s].scene.accel) + offsetof(rt_accel_header, build_flags);
+        RT_CUDA_CTX(ctx, cudaMemcpy(&bf, src, sizeof(bf), cudaMemcpyDeviceToHost));
+        const uint32_t w = (bf & RT_BUILD_WIDTH_MASK) >> 16;
+        cur.bvh_width = w ? w : 8u;
+        break;
+    }
     float cur_ms = 0.0f;
     rc = time_tuning(ctx, scenes, n_scenes, &tp, cur, scratch, scratch_bytes, tm, &cur_ms);
     if (rc) return rc == RT_ERR_BOUNDS ? rc : rtc::set_error(ctx, rc, "rt_batch_autotune: the default tuning failed");

@@ -50,6 +50,13 @@ struct BuildLayout {
 
 inline uint32_t node_capacity_for(uint32_t n) { return n < 2 ? 1u : n - 1u; }
 
+// Children per wide node from the build flags (0 = 8); 0 when invalid.
+inline uint32_t build_width(uint32_t flags) {
+    const uint32_t w = (flags & RT_BUILD_WIDTH_MASK) >> 16;
+    if (w == 0u) return 8u;
+    return (w >= 4u && w <= 8u) ? w : 0u;
+}
+
 BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
     BuildLayout L;
     uint64_t off = 0;
@@ -461,6 +468,7 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
 
 struct CollapseArgs {
     uint32_t n;
+    uint32_t width;      // children per wide node, 4..8
     uint32_t rec_words;  // uint4 words per leaf record (3 or 5)
     uint32_t capacity;
     uint32_t root_ref;
@@ -494,7 +502,7 @@ __device__ int collapse_children(const CollapseArgs &a, uint32_t src, uint32_t o
     int n = 2;
     out[0] = nd.x;
     out[1] = nd.y;
-    while (n < 8) {
+    while (n < (int)a.width) {
         int best = -1;
         float best_a = -1.0f;
         for (int i = 0; i < n; ++i) {
@@ -792,6 +800,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     const int bpa = (bc.flags & RT_BUILD_MORTON30) ? 10 : 21;
     const int passes = bpa == 10 ? 4 : 8;
     const uint32_t n = bc.n;
+    if (build_width(bc.flags) == 0u) return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_WIDTH must be 4..8");
     BuildLayout L = build_layout(n, bc.rec_bytes, passes);
     if (out_layout) *out_layout = L;
     const uint64_t need_accel =
@@ -882,6 +891,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
 
     CollapseArgs ca;
     ca.n = n;
+    ca.width = build_width(bc.flags);
     ca.rec_words = bc.rec_bytes / 16u;
     ca.capacity = cap;
     ca.root_ref = n >= 2 ? 0u : (kLeafBit | 0u);

@@ -913,7 +913,7 @@ int batch_tuning(const rt_batch_tuning *in, rt_batch_tuning *out) {
     if ((t.trace_threads != 128u && t.trace_threads != 256u) ||
         (t.stack_ring != 8u && t.stack_ring != 16u && t.stack_ring != 32u) || t.refill > 32u ||
         t.trace_blocks_per_sm > 64u || (t.shade_threads != 128u && t.shade_threads != 256u && t.shade_threads != 512u) ||
-        t.bvh_width != 8u)
+        t.bvh_width < 4u || t.bvh_width > 8u)
         return RT_ERR_INVALID_ARG;
     *out = t;
     return RT_OK;
@@ -1089,7 +1089,7 @@ extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene 
     if (batch_tuning(t, &tt))
         return set_error(ctx, RT_ERR_INVALID_ARG,
                          "rt_batch_plan_create: tuning needs 128/256 trace threads, ring 8/16/32, refill <= 32, "
-                         "128/256/512 shade threads, BVH width 8");
+                         "128/256/512 shade threads, BVH width 4..8");
     const uint64_t cap = (tt.wave_paths && tt.wave_paths < P) ? tt.wave_paths : P;
     const BtLayout L = bt_layout(n_scenes, NL, cap);
     if (scratch_bytes < L.total)

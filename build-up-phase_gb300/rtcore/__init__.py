@@ -36,6 +36,7 @@ RT_ERR_NOT_FOUND = -8
 STATUS_NAMES = {0: "RT_OK", -1: "RT_ERR_INVALID_ARG", -2: "RT_ERR_OOM", -3: "RT_ERR_CUDA",
                 -4: "RT_ERR_TIMEOUT", -5: "RT_ERR_BOUNDS", -6: "RT_ERR_UNSUPPORTED",
                 -7: "RT_ERR_NO_DEVICE", -8: "RT_ERR_NOT_FOUND"}
+RT_BUILD_WIDTH_MASK = 0xF << 16
 RT_BATCH_GRAPH = 1
 RT_BATCH_DISCARD = 2
 RT_TUNE_FORCE = 1
@@ -562,6 +563,11 @@ def tuning_cache_store(path, key: str, t: BatchTuning, ms: float) -> None:
     rc = load().rt_batch_tuning_cache_store(os.fsencode(str(path)), key.encode(), C.byref(t), ms)
     if rc != RT_OK:
         raise RtError(rc, "rt_batch_tuning_cache_store")
+
+
+def build_width(w: int) -> int:
+    """RT_BUILD_WIDTH(w): build flag for at most w children per wide node (4..8)."""
+    return (w & 0xF) << 16
 
 
 def refit_scratch_bytes(prim_count: int) -> int:

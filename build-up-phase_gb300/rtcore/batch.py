@@ -4,14 +4,18 @@ rt_path_trace launch per scene.
 
     python -m rtcore.batch [--scenes 64] [--min-tris 10000] [--max-tris 5000000]
                            [--spp 16] [--depth 8] [--tune-cache FILE] [--retune]
-                           [--repeat 2] [--out result.json]
+                           [--widths 4,6,8] [--repeat 2] [--out result.json]
 
 Scenes (seed 0x5EED0004): each is a lit triangle soup or a box scene with
 probability 1/2, triangle count exp(U(ln min, ln max)), square resolution
 drawn from {512, 1024, 1536, 2048}, its own jittered camera.  Both forms trace
 the same samples (the batch adds to each scene's image exactly what
 rt_path_trace adds), so their times compare equal work; the batch's launch
-shapes come from the autotuner (rt_batch_autotune) and its JSON cache.
+shapes come from the autotuner (rt_batch_autotune) and its JSON cache.  With
+--retune and more than one --widths value, the BVH width is tuned too: every
+scene is rebuilt with RT_BUILD_WIDTH(w) for each w and one-sample graph
+launches of the tuned shape are timed; the fastest width is stored with the
+launch shapes.
 """
 from __future__ import annotations
 
@@ -26,8 +30,8 @@ from pathlib import Path
 
 import numpy as np
 
-from . import (BatchParams, BatchScene, Camera, Context, GeometryTriangles, PtParams, PtScene, default_batch_tuning,
-               load)
+from . import (BatchParams, BatchScene, Camera, Context, GeometryTriangles, PtParams, PtScene, build_width,
+               default_batch_tuning, load, tuning_cache_lookup, tuning_cache_store)
 from . import scenes as S
 
 BATCH_SEED = S.SEED_BASE + 4
@@ -110,30 +114,41 @@ class GpuScene:
     """One scene on the device: bottom-level structure, materials, lights and
     its accumulation image."""
 
-    def __init__(self, ctx: Context, spec: SceneSpec, host, scratch=None):
+    def __init__(self, ctx: Context, spec: SceneSpec, host, scratch=None, width: int = 8):
         import torch
         v, i, tm, m = host
         self.spec = spec
         self.n_tris = len(i)
         lights = S.emissive_lights(v, i, tm, m)
         self.n_lights = len(lights)
-        dv = torch.from_numpy(np.ascontiguousarray(v).reshape(-1)).cuda()
-        di = torch.from_numpy(np.ascontiguousarray(i).reshape(-1).view(np.int32)).cuda()
+        # the geometry stays on the device for rebuilds with another width
+        self.dv = torch.from_numpy(np.ascontiguousarray(v).reshape(-1)).cuda()
+        self.di = torch.from_numpy(np.ascontiguousarray(i).reshape(-1).view(np.int32)).cuda()
+        self.n_vertices = len(v)
         self.keep = [torch.from_numpy(tm.view(np.int32)).cuda(), torch.from_numpy(m.view(np.uint8)).cuda(),
                      torch.from_numpy(lights.view(np.uint8)).cuda()]
-        g = GeometryTriangles()
-        g.vertices, g.vertex_stride, g.max_vertex = dv.data_ptr(), 12, len(v) - 1
-        g.index_type, g.indices, g.tri_count, g.flags = 1, di.data_ptr(), len(i), 1
         sz = ctx.blas_sizes([len(i)])
         self.accel = torch.empty(sz.accel_bytes, dtype=torch.uint8, device="cuda")
-        if scratch is None or scratch.numel() < sz.scratch_bytes:
-            scratch = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device="cuda")
-        ctx.build_blas([g], 0, self.accel, sz.accel_bytes, scratch, sz.scratch_bytes)
-        ctx.sync()
-        self.scratch = scratch  # reusable by the next build
+        self.scratch = self.build(ctx, width, scratch)  # reusable by the next build
         self.accum = torch.zeros(spec.width * spec.height * 4, dtype=torch.float32, device="cuda")
         self.pt = PtScene(ctx.address(self.accel), self.keep[0].data_ptr(), self.keep[1].data_ptr(), len(m),
                           self.keep[2].data_ptr(), len(lights))
+
+    def build(self, ctx: Context, width: int = 8, scratch=None):
+        """(Re)builds the structure with at most `width` children per node;
+        returns the scratch buffer used (for reuse)."""
+        import torch
+        g = GeometryTriangles()
+        g.vertices, g.vertex_stride, g.max_vertex = self.dv.data_ptr(), 12, self.n_vertices - 1
+        g.index_type, g.indices, g.tri_count, g.flags = 1, self.di.data_ptr(), self.n_tris, 1
+        sz = ctx.blas_sizes([self.n_tris])
+        if scratch is None or scratch.numel() < sz.scratch_bytes:
+            scratch = torch.empty(sz.scratch_bytes, dtype=torch.uint8, device="cuda")
+        ctx.build_blas([g], build_width(width) if width != 8 else 0, self.accel, sz.accel_bytes, scratch,
+                       sz.scratch_bytes)
+        ctx.sync()
+        self.bvh_width = width
+        return scratch
 
     def camera(self) -> Camera:
         return Camera(self.spec.camera[0], self.spec.camera[1])
@@ -145,18 +160,46 @@ class GpuScene:
         return PtParams(self.camera(), self.spec.width, self.spec.height, spp, offset, depth, rr, seed, eps, 0)
 
 
-def build_scenes(ctx: Context, specs: list[SceneSpec], threads: int | None = None) -> list[GpuScene]:
+def build_scenes(ctx: Context, specs: list[SceneSpec], threads: int | None = None, width: int = 8) -> list[GpuScene]:
     """Generates the scenes on host threads (the generators release the GIL)
     and builds their structures on the device, in order."""
     threads = threads or min(16, os.cpu_count() or 4)
     out, scratch = [], None
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         for spec, host in zip(specs, ex.map(host_scene, specs)):
-            sc = GpuScene(ctx, spec, host, scratch)
+            sc = GpuScene(ctx, spec, host, scratch, width)
             scratch = sc.scratch
             sc.scratch = None
             out.append(sc)
     return out
+
+
+def rebuild_scenes(ctx: Context, scenes: list[GpuScene], width: int) -> None:
+    scratch = None
+    for sc in scenes:
+        if sc.bvh_width != width:
+            scratch = sc.build(ctx, width, scratch)
+
+
+def sweep_widths(ctx: Context, scenes: list[GpuScene], p: BatchParams, tuning, scratch, nb: int, widths,
+                 stream) -> dict:
+    """{width: ms of one sample per pixel} with the given launch shape, best of
+    three graph launches after a warm-up (results discarded); the scenes are
+    left built with the fastest width."""
+    import torch
+    one = BatchParams(1, p.max_depth, p.rr_depth, 0, p.seed, p.ray_eps, 0)
+    times = {}
+    for w in widths:
+        rebuild_scenes(ctx, scenes, w)
+        t = type(tuning).from_buffer_copy(tuning)
+        t.bvh_width = w
+        plan = ctx.batch_plan([sc.batch_scene() for sc in scenes], one, scratch, nb, t, graph=True, discard=True)
+        plan.launch(0, stream)
+        times[w] = min(time_ms(lambda: plan.launch(0, stream), stream) for _ in range(3))
+        plan.close()
+        torch.cuda.synchronize()
+    rebuild_scenes(ctx, scenes, min(times, key=times.get))
+    return times
 
 
 def batch_params(spp: int, depth: int = 8, seed: int = BATCH_SEED, rr: int = 3, eps: float = 1e-4) -> BatchParams:
@@ -178,6 +221,16 @@ class Sequential:
                                 self.nb, stream)
 
 
+def _record_width_trials(path, key: str, width_ms: dict) -> None:
+    """Adds the width sweep's times to the key's entry of the tuning cache."""
+    p = Path(path)
+    doc = json.loads(p.read_text())
+    doc["entries"][key]["width_trials"] = [[f"bvh width {w}", round(ms, 3)] for w, ms in sorted(width_ms.items())]
+    tmp = p.with_name(p.name + f".tmp.{os.getpid()}")
+    tmp.write_text(json.dumps(doc, indent=2) + "\n")
+    os.replace(tmp, p)
+
+
 def time_ms(fn, stream) -> float:
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -197,6 +250,7 @@ def main(argv=None) -> int:
     ap.add_argument("--depth", type=int, default=8)
     ap.add_argument("--tune-cache", default=str(DEFAULT_CACHE))
     ap.add_argument("--retune", action="store_true")
+    ap.add_argument("--widths", default="8", help="BVH widths to tune over with --retune, e.g. 4,6,8")
     ap.add_argument("--repeat", type=int, default=2, help="timed launches of each form (after one warm-up)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
@@ -214,6 +268,18 @@ def main(argv=None) -> int:
     scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
     t1 = time.time()
     tuning, tune_ms = ctx.batch_autotune(table, p, scratch, nb, a.tune_cache, force=a.retune)
+    widths = sorted({int(w) for w in a.widths.split(",")})
+    width_ms = None
+    key = ctx.batch_tuning_key(table, p)
+    if a.retune and len(widths) > 1:
+        width_ms = sweep_widths(ctx, scenes, p, tuning, scratch, nb, widths, st)
+        best = min(width_ms, key=width_ms.get)
+        tuning.bvh_width = best
+        tuning_cache_store(a.tune_cache, key, tuning, width_ms[best])
+        _record_width_trials(a.tune_cache, key, width_ms)
+    elif tuning.bvh_width != 8:
+        rebuild_scenes(ctx, scenes, tuning.bvh_width)
+    table = [sc.batch_scene() for sc in scenes]
     t_tune = time.time() - t1
     plan = ctx.batch_plan(table, p, scratch, nb, tuning, graph=True)
     seq = Sequential(ctx, scenes, a.spp, a.depth)
@@ -232,7 +298,8 @@ def main(argv=None) -> int:
     res = {
         "scenes": len(specs), "tris": int(sum(sc.n_tris for sc in scenes)), "pixels": pixels, "spp": a.spp,
         "depth": a.depth, "build_wall_s": round(t_build, 1), "tune_wall_s": round(t_tune, 1),
-        "tuning": tuning.as_dict(), "tuning_key": ctx.batch_tuning_key(table, p), "tuning_1spp_ms": round(tune_ms, 3),
+        "tuning": tuning.as_dict(), "tuning_key": key, "tuning_1spp_ms": round(tune_ms, 3),
+        "width_1spp_ms": {str(k): round(v, 3) for k, v in width_ms.items()} if width_ms else None,
         "graph_kernels": plan.launches(),
         "batch_ms": [round(x, 3) for x in batch_ms], "sequential_ms": [round(x, 3) for x in seq_ms],
         "rays_per_launch": {"extension": ext, "shadow": shadow},

@@ -103,6 +103,11 @@ enum {
     RT_BUILD_MORTON30 = 1u << 8,          /* 30-bit keys, 4 sort passes */
     RT_BUILD_MORTON63 = 1u << 9           /* 63-bit keys, 8 passes (default) */
 };
+/* Children per wide node: RT_BUILD_WIDTH(w), w in 4..8 (bits 16-19; 0 = 8).
+ * The node format stays the 8-slot one; a narrower tree is deeper with fewer
+ * child tests per node. */
+#define RT_BUILD_WIDTH(w) ((uint32_t)(w) << 16)
+#define RT_BUILD_WIDTH_MASK (0xfu << 16)
 
 /* vkGetAccelerationStructureBuildSizesKHR output (main.cpp:756-762). */
 typedef struct rt_build_sizes {

@@ -60,7 +60,11 @@ typedef struct rt_batch_tuning {
     uint32_t wave_paths;           /* paths in flight per wave (the queue
                                       capacity); 0 = every pixel of every
                                       scene in one wave                      */
-    uint32_t bvh_width;            /* 8: the node format of rtcore_accel.h  */
+    uint32_t bvh_width;            /* children per node the scenes'
+                                      structures were built with
+                                      (RT_BUILD_WIDTH, 4..8): a build-time
+                                      choice recorded with the launch shapes;
+                                      the plan traces any width              */
     uint32_t reserved;
 } rt_batch_tuning;
 
@@ -110,6 +114,8 @@ rt_status rt_batch_plan_destroy(rt_batch_plan *plan);
  * walking one parameter at a time from the defaults and keeping each
  * improvement of more than 1 %, and returns the fastest in *best (its time in
  * *best_ms).
+ * The returned bvh_width is the width the structures were built with; the
+ * width itself is chosen by rebuilding and timing (rtcore.batch --widths).
  * With a cache_path, the result is looked up first and stored after tuning
  * in a JSON file keyed by rt_batch_tuning_key; flags RT_TUNE_FORCE re-tunes
  * even when the key is present.  scratch: rt_batch_scratch_bytes(..., NULL).
@@ -127,8 +133,9 @@ rt_status rt_batch_tuning_key(rt_context *ctx, const rt_batch_scene *scenes, uin
                               const rt_batch_params *p, char *key, uint32_t key_bytes);
 
 /* The JSON tuning cache (host only): lookup returns RT_ERR_NOT_FOUND when the
- * file or the key is absent; store adds or replaces the key's entry and
- * rewrites the file atomically. */
+ * file or the key is absent; store adds the key's entry or updates its
+ * tuning fields and time (keeping its other fields, such as the autotuner's
+ * trial list) and rewrites the file atomically. */
 rt_status rt_batch_tuning_cache_lookup(const char *path, const char *key, rt_batch_tuning *t, float *ms);
 rt_status rt_batch_tuning_cache_store(const char *path, const char *key, const rt_batch_tuning *t, float ms);
 

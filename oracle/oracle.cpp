@@ -356,12 +356,12 @@ Tree build_tree(const BuildInput &in, uint32_t flags, uint32_t &morton_bits, orc
 /* Children of the wide node whose source is binary reference `src`:
  * greedy opening of the largest-area openable child (SAH leaf decisions
  * fixed in the binary tree). */
-int collapse_children(const Tree &t, uint32_t src, uint32_t out[8]) {
+int collapse_children(const Tree &t, uint32_t src, uint32_t out[8], int width) {
     if (!ref_openable(t, src)) { out[0] = src; return 1; }
     int n = 2;
     out[0] = t.nodes[src].left;
     out[1] = t.nodes[src].right;
-    while (n < 8) {
+    while (n < width) {
         int best = -1;
         float best_a = -1.0f;
         for (int i = 0; i < n; ++i) {
@@ -445,6 +445,8 @@ void write_node(rt_bvh8_node &nd, const Box &node, const Box *slot_box, const bo
 
 BuildResult build_wide(const BuildInput &in, uint32_t flags, orc_lbvh_debug *dbg) {
     BuildResult res;
+    const uint32_t wf = (flags & RT_BUILD_WIDTH_MASK) >> 16;
+    const int width = wf ? (int)wf : 8;
     Tree t = build_tree(in, flags, res.morton_bits, dbg);
     uint32_t n = in.n;
     res.prims.resize((size_t)n * in.rec_bytes);
@@ -473,7 +475,7 @@ BuildResult build_wide(const BuildInput &in, uint32_t flags, orc_lbvh_debug *dbg
         for (size_t k = 0; k < level.size(); ++k) {
             uint32_t src = level[k];
             uint32_t ch[8];
-            int nc = collapse_children(t, src, ch);
+            int nc = collapse_children(t, src, ch, width);
             Box cb[8];
             for (int c = 0; c < nc; ++c) cb[c] = ref_box(t, ch[c]);
             Box nbox = ref_box(t, src);
@@ -961,8 +963,14 @@ uint64_t orc_tlas_accel_bytes(uint32_t n_instances) {
     return align256(RT_ACCEL_HEADER_BYTES + cap * 80u + (uint64_t)n_instances * 80u);
 }
 
+inline bool width_ok(uint32_t flags) {
+    const uint32_t w = (flags & RT_BUILD_WIDTH_MASK) >> 16;
+    return w == 0u || (w >= 4u && w <= 8u);
+}
+
 int orc_build_blas(const orc_geometry *geoms, uint32_t n_geoms, uint32_t flags, void *accel, uint64_t accel_bytes,
                    orc_lbvh_debug *dbg) {
+    if (!width_ok(flags)) return RT_ERR_INVALID_ARG;
     std::vector<uint32_t> counts(n_geoms);
     for (uint32_t g = 0; g < n_geoms; ++g) counts[g] = geoms[g].tri_count;
     uint64_t need = orc_blas_accel_bytes(counts.data(), n_geoms);
@@ -977,6 +985,7 @@ int orc_build_blas(const orc_geometry *geoms, uint32_t n_geoms, uint32_t flags, 
 }
 
 int orc_build_tlas(const rt_instance *instances, uint32_t n, uint32_t flags, void *accel, uint64_t accel_bytes) {
+    if (!width_ok(flags)) return RT_ERR_INVALID_ARG;
     uint64_t need = orc_tlas_accel_bytes(n);
     if (accel_bytes < need) return RT_ERR_OOM;
     BuildInput in;

@@ -48,7 +48,7 @@ def test_scratch_sizing_and_validation(rtlib):
     t.wave_paths = 10 ** 9  # larger than the batch: one wave
     assert _scratch_bytes(rtlib, scenes, t) == (rtcore.RT_OK, full)
     for field, value in (("stack_ring", 12), ("trace_threads", 64), ("refill", 33), ("shade_threads", 1024),
-                         ("bvh_width", 4)):
+                         ("bvh_width", 3), ("bvh_width", 9)):
         bad = rtcore.default_batch_tuning()
         setattr(bad, field, value)
         assert _scratch_bytes(rtlib, scenes, bad)[0] == rtcore.RT_ERR_INVALID_ARG, field
@@ -88,11 +88,15 @@ def test_tuning_cache_roundtrip(rtlib, tmp_path):
     assert t.as_dict() == a.as_dict() and abs(ms - 12.346) < 1e-4
     t, ms = rtcore.tuning_cache_lookup(path, "other \"quoted\" key")
     assert t.as_dict() == b.as_dict() and ms == 1.5
-    # replacing an entry keeps the others
+    # updating an entry keeps the other entries and the entry's other fields
+    doc = json.loads(path.read_text())
+    doc["entries"]["sm103-152/n2^6/tris2^25/px2^27/d8"]["trials"] = [["x", 1.0]]
+    path.write_text(json.dumps(doc))
     a.refill = 2
     rtcore.tuning_cache_store(path, "sm103-152/n2^6/tris2^25/px2^27/d8", a, 10.0)
     doc = json.loads(path.read_text())
-    assert len(doc["entries"]) == 2 and doc["entries"]["sm103-152/n2^6/tris2^25/px2^27/d8"]["refill"] == 2
+    e = doc["entries"]["sm103-152/n2^6/tris2^25/px2^27/d8"]
+    assert len(doc["entries"]) == 2 and e["refill"] == 2 and e["ms"] == 10 and e["trials"] == [["x", 1]]
     assert not list(tmp_path.glob("*.tmp.*"))
 
 

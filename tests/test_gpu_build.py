@@ -29,6 +29,28 @@ def test_blas_bit_exact(ctx, orc, n, flags):
     compare_accels(g.bytes(), o, 48)
 
 
+@pytest.mark.parametrize("n", [9, 20000, 250000])
+@pytest.mark.parametrize("width", [4, 6])
+def test_narrow_blas_bit_exact(ctx, orc, n, width):
+    """RT_BUILD_WIDTH(4..7): trees of at most `width` children per node,
+    byte-identical to the oracle's."""
+    import rtcore
+    items = soup(n, seed=8)
+    flags = rtcore.build_width(width)
+    g = GpuBlas(ctx, items, flags)
+    o, rc = orc.build_blas(items, flags)
+    assert rc == 0
+    compare_accels(g.bytes(), o, 48)
+
+
+def test_invalid_width_rejected(ctx):
+    import rtcore
+    for w in (2, 3, 9):
+        with pytest.raises(rtcore.RtError) as e:
+            GpuBlas(ctx, soup(50), rtcore.build_width(w))
+        assert e.value.code == rtcore.RT_ERR_INVALID_ARG
+
+
 def test_blas_stages_bit_exact(ctx, orc):
     import rtcore
     n = 50000

@@ -80,9 +80,13 @@ def test_refit_rejects_other_inputs(ctx, orc):
         g.refit(ctx, [(v[:597], i[:199], None)])  # one triangle fewer
     assert e.value.code == rtcore.RT_ERR_INVALID_ARG
     assert g.bytes().tobytes() == before.tobytes()
-    with pytest.raises(rtcore.RtError) as e:
-        g.refit(ctx, [(v, i, None), (v, i, None)])  # another geometry count
+    with pytest.raises(rtcore.RtError) as e:  # the same 200 triangles as two geometries
+        g.refit(ctx, [(v[:300], i[:100], None), (v[300:], i[100:] - 300, None)])
     assert e.value.code == rtcore.RT_ERR_INVALID_ARG
+    assert g.bytes().tobytes() == before.tobytes()
+    with pytest.raises(rtcore.RtError) as e:  # more triangles than the structure holds: refused on the host
+        g.refit(ctx, [(v, i, None), (v, i, None)])
+    assert e.value.code == rtcore.RT_ERR_OOM
     assert g.bytes().tobytes() == before.tobytes()
 
 

@@ -84,3 +84,30 @@ def test_mismatched_inputs_are_rejected(orc):
     assert orc.refit_blas(a, [(v[:297], i[:99], None)]) == rtcore.RT_ERR_INVALID_ARG  # one triangle fewer
     assert orc.refit_blas(a, [(v, i, None), (v, i, None)]) == rtcore.RT_ERR_INVALID_ARG  # two geometries
     assert a.tobytes() == before
+
+
+@pytest.mark.parametrize("width", [4, 5, 6, 8])
+def test_narrow_trees(orc, width):
+    """RT_BUILD_WIDTH(w): at most w children per node, the same hits."""
+    import rtcore
+    from helpers import nodes
+    v, i = _soup(3000)
+    a, rc = orc.build_blas([(v, i, None)], rtcore.build_width(width))
+    assert rc == 0
+    nd = nodes(a)
+    children = np.array([bin(int(im)).count("1") for im in nd["imask"]]) + \
+        np.array([sum(1 for s in range(8) if m[s] and not (im >> s) & 1) for m, im in zip(nd["meta"], nd["imask"])])
+    assert children.max() <= width and children.max() >= min(width, 4)
+    rays = _rays(orc, 2000)
+    assert orc.trace_closest(a, rays)[0].tobytes() == orc.brute_closest([(v, i, None)], rays, 32).tobytes()
+    if width < 8:
+        a8, _ = orc.build_blas([(v, i, None)])
+        assert len(nodes(a8)) < len(nd)
+
+
+def test_invalid_width_rejected(orc):
+    import rtcore
+    v, i = _soup(10)
+    for w in (1, 2, 3, 9, 15):
+        _, rc = orc.build_blas([(v, i, None)], rtcore.build_width(w))
+        assert rc == rtcore.RT_ERR_INVALID_ARG, w
