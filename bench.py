@@ -481,9 +481,14 @@ def secondary_workloads(ctx, stream, dev) -> dict:
     ctx.path_trace(sc, p, acc, pscr, nb, stream)
     ms_pt = _events(torch, stream, lambda: ctx.path_trace(sc, p, acc, pscr, nb, stream), 3)
     ext, shadow = ctx.pt_ray_counts(p, len(lights), pscr, stream)
+    # the same samples with the bounce rays grouped by direction octant
+    pu = rtcore.PtParams(p.camera, W, H, 4, 0, 8, 3, S.SEED_BASE + 3, 1e-4, rtcore.RT_PT_OCTANT_BINNING)
+    ctx.path_trace(sc, pu, acc, pscr, nb, stream)
+    ms_pu = _events(torch, stream, lambda: ctx.path_trace(sc, pu, acc, pscr, nb, stream), 3)
     out["path_tracer"] = {"resolution": [W, H], "spp_per_call": 4, "ms_per_spp": round(ms_pt / 4, 3),
                           "mrays_per_s": round((ext + shadow) / ms_pt / 1e3, 1),
-                          "rays_per_spp": round((ext + shadow) / 4 / n, 3)}
+                          "rays_per_spp": round((ext + shadow) / 4 / n, 3),
+                          "ms_per_spp_octant_binning": round(ms_pu / 4, 3)}
     del pscr, acc
     # MLP cache: 2M queries (43,520 FLOP each, algorithmic) and 65,536 training
     # samples per pass (120,192 FLOP each)

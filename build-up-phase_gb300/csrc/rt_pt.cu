@@ -44,16 +44,23 @@ constexpr float kRrMax = 0.95f;
 
 struct PtLayout {
     uint64_t rays0, rays1, pidx0, pidx1, hits, srays, spidx, scontrib, socc, tput, rad, rng, light_aux, light_cdf,
-        counters, total;
+        counters, stage, stage_pidx, stage_rank, total;
     // learned form: cache queries at the second vertex and training samples
     uint64_t qin, qout, qt1, qpidx, tin, ttarget, tt1, tlpre, tpidx;
     uint32_t cap, train_cap;
 };
 
 // counter words of the scratch counter block
-constexpr uint32_t kCntQuery = 257, kCntTrain = 258, kCntPerSample = 259;  // words [0, 259) reset per sample
-constexpr uint32_t kCntRays = 260;    // two u64
-constexpr uint32_t kCntSample = 270;  // sample index of the running wave
+// Counter block (32-bit words): [0, 65) extension queue lengths per depth,
+// [65, 129) shadow queue lengths, [129, 257) traversal work counters,
+// 257 cache queries, 258 training samples, [259, 779) extension rays per
+// direction octant per depth -- all reset per sample -- then two u64 ray
+// counts and the sample index of the running wave.
+constexpr uint32_t kCntQuery = 257, kCntTrain = 258, kCntBins = 259;
+constexpr uint32_t kCntPerSample = kCntBins + 8u * 65u;  // 779
+constexpr uint32_t kCntRays = 780;    // two u64 (8-byte aligned)
+constexpr uint32_t kCntSample = 784;  // sample index of the running wave
+constexpr uint32_t kCntWords = 800;
 
 PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap = 0) {
     PtLayout L;
@@ -79,10 +86,10 @@ PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap 
     L.rng = take(cap * 8u);
     L.light_aux = take((uint64_t)(n_lights ? n_lights : 1) * 16u);
     L.light_cdf = take((uint64_t)(n_lights ? n_lights : 1) * 4u + 16u);
-    // counters: [0, 65) queue lengths per vertex, [65, 129) shadow lengths,
-    // [129, 257) traversal work counters, 257 cache queries, 258 training
-    // samples, 260.. two u64 ray counts (8-byte aligned), 270 sample index
-    L.counters = take(272u * 4u);
+    L.counters = take(kCntWords * 4u);
+    L.stage = take(cap * 32u);
+    L.stage_pidx = take(cap * 4u);
+    L.stage_rank = take(cap * 4u);
     L.train_cap = train_cap;
     const uint64_t qcap = train_cap ? cap : 0;
     L.qin = take(qcap * 48u);
@@ -171,6 +178,15 @@ struct PtArgs {
     float4 *tlpre;
     uint32_t *tpidx;
     uint32_t *tcount;
+    // octant binning of the extension rays: shade writes them to the stage
+    // arrays with their rank within their octant, the scatter kernel places
+    // them octant by octant
+    uint32_t binning;
+    float4 *stage;
+    uint32_t *stage_pidx;
+    uint32_t *stage_rsid;
+    uint32_t *stage_rank;
+    uint32_t *bins_out;   // the 8 octant counters of the next depth
     // batch (multi-scene kernels): each queue entry carries its scene
     const BtScene *bt;
     uint32_t wave_base;        // global path index of slot 0 of the wave
@@ -246,6 +262,42 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *count, unsi
     }
     base = __shfl_sync(0xffffffffu, base, leader);
     return want ? base + (uint32_t)__popc(mask & ((1u << lane) - 1u)) : 0xffffffffu;
+}
+
+// Direction octant: bit k set when component k is negative.
+__device__ __forceinline__ uint32_t octant_of(const float d[3]) {
+    return (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+}
+
+// Places the staged extension rays octant by octant: ray i goes to the start
+// of its octant's range (prefix of the 8 counts) plus its rank in the octant.
+template <bool MULTI>
+__global__ void __launch_bounds__(512) k_pt_bin_scatter(const uint32_t *count, const uint32_t *bins,
+                                                         const float4 *stage, const uint32_t *stage_pidx,
+                                                         const uint32_t *stage_rsid, const uint32_t *stage_rank,
+                                                         float4 *rays_out, uint32_t *pidx_out, uint32_t *rsid_out,
+                                                         uint32_t cap, uint32_t *err) {
+    const uint32_t n = *count;
+    uint32_t start[8];
+    uint32_t acc = 0;
+    for (int b = 0; b < 8; ++b) {
+        start[b] = acc;
+        acc += bins[b];
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 r0 = stage[2u * i], r1 = stage[2u * i + 1u];
+        const float d[3] = {r1.x, r1.y, r1.z};
+        const uint32_t b = octant_of(d);
+        const uint32_t dst = start[b] + stage_rank[i];
+        if (dst >= n || dst >= cap) {  // the counts disagree: a broken invariant, never an out-of-range write
+            report_error(err, RT_ERR_BOUNDS, 0x79000000u | (i & 0xffffffu));
+            continue;
+        }
+        rays_out[2u * dst] = r0;
+        rays_out[2u * dst + 1u] = r1;
+        pidx_out[dst] = stage_pidx[i];
+        if (MULTI) rsid_out[dst] = stage_rsid[i];
+    }
 }
 
 // Shades queue entry i (all 32 lanes of the warp call it together: the
@@ -429,7 +481,25 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
         if (MULTI) a.ssid[sslot] = sid;
     }
     const uint32_t nslot = warp_append(want_next, a.count_out, a.ray_counts);
-    if (want_next) {
+    if (a.binning) {
+        // rank within the ray's direction octant: lanes of one octant (match_any)
+        // take their slots with one atomic on the octant's counter
+        const uint32_t wm = __ballot_sync(0xffffffffu, want_next);
+        if (want_next) {
+            const uint32_t bin = octant_of(nd);
+            const uint32_t peers = __match_any_sync(wm, bin);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.bins_out + bin, (uint32_t)__popc(peers));
+            base = __shfl_sync(wm, base, leader);
+            a.stage[2u * nslot] = make_float4(no[0], no[1], no[2], 0.0f);
+            a.stage[2u * nslot + 1u] = make_float4(nd[0], nd[1], nd[2], 1e30f);
+            a.stage_pidx[nslot] = p;
+            if (MULTI) a.stage_rsid[nslot] = sid;
+            a.stage_rank[nslot] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        }
+    } else if (want_next) {
         a.rays_out[2u * nslot] = make_float4(no[0], no[1], no[2], 0.0f);
         a.rays_out[2u * nslot + 1u] = make_float4(nd[0], nd[1], nd[2], 1e30f);
         a.pidx_out[nslot] = p;
@@ -724,6 +794,11 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
     const unsigned blocks = (unsigned)((npix + kPtThreads - 1) / kPtThreads);
     const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<false>, kPtThreads, npix);
     const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, kPtThreads, npix);
+    const unsigned scatter_blocks = resident_blocks(ctx, (const void *)k_pt_bin_scatter<false>, kPtThreads, npix);
+    a.binning = (p->flags & RT_PT_OCTANT_BINNING) ? 1u : 0u;
+    a.stage = reinterpret_cast<float4 *>(S + L.stage);
+    a.stage_pidx = reinterpret_cast<uint32_t *>(S + L.stage_pidx);
+    a.stage_rank = reinterpret_cast<uint32_t *>(S + L.stage_rank);
 
     for (uint32_t s = 0; s < p->spp; ++s) {
         RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
@@ -744,8 +819,15 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
             a.count_out = &cnt[d + 1];
             a.scount = &scnt[d];
             a.depth = d;
+            a.bins_out = cnt + kCntBins + 8u * (d + 1u);
             k_pt_shade<false><<<shade_blocks, kPtThreads, 0, st>>>(a);
             RT_CUDA_CTX(ctx, cudaGetLastError());
+            if (a.binning && d + 1u < p->max_depth) {
+                k_pt_bin_scatter<false><<<scatter_blocks, kPtThreads, 0, st>>>(
+                    &cnt[d + 1], a.bins_out, a.stage, a.stage_pidx, nullptr, a.stage_rank, rays[q ^ 1u],
+                    pidx[q ^ 1u], nullptr, (uint32_t)npix, ctx->d_err);
+                RT_CUDA_CTX(ctx, cudaGetLastError());
+            }
             rc = launch_queue_trace(ctx, st, accel, a.srays, nullptr, socc, &scnt[d], (uint32_t)npix,
                                     &tcnt[2 * d + 1], true);
             if (rc) return rc;
@@ -827,6 +909,7 @@ namespace {
 struct BtLayout {
     uint64_t table, views, light_aux, light_cdf, counters;
     uint64_t rays0, rays1, pidx0, pidx1, rsid0, rsid1, hits, srays, spidx, ssid, scontrib, socc, tput, rad, rng, psid;
+    uint64_t stage, stage_pidx, stage_rsid, stage_rank;
     uint64_t total;
     uint64_t cap;  // paths per wave
 };
@@ -844,7 +927,7 @@ BtLayout bt_layout(uint32_t n_scenes, uint64_t n_lights, uint64_t cap) {
     L.views = take((uint64_t)n_scenes * sizeof(TravScene));
     L.light_aux = take(n_lights * 16u);
     L.light_cdf = take((n_lights + n_scenes) * 4u);
-    L.counters = take(272u * 4u);  // word layout of the single-scene path tracer
+    L.counters = take(kCntWords * 4u);  // word layout of the single-scene path tracer
     L.rays0 = take(cap * 32u);
     L.rays1 = take(cap * 32u);
     L.pidx0 = take(cap * 4u);
@@ -861,6 +944,10 @@ BtLayout bt_layout(uint32_t n_scenes, uint64_t n_lights, uint64_t cap) {
     L.rad = take(cap * 16u);
     L.rng = take(cap * 8u);
     L.psid = take(cap * 4u);
+    L.stage = take(cap * 32u);
+    L.stage_pidx = take(cap * 4u);
+    L.stage_rsid = take(cap * 4u);
+    L.stage_rank = take(cap * 4u);
     L.total = off;
     return L;
 }
@@ -989,6 +1076,11 @@ int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
     const uint64_t W = L.cap;
     const uint64_t waves = (pl->paths + W - 1u) / W;
     const uint32_t discard = (pl->flags & RT_BATCH_DISCARD) ? 1u : 0u;
+    a.binning = (pl->p.flags & RT_PT_OCTANT_BINNING) ? 1u : 0u;
+    a.stage = reinterpret_cast<float4 *>(S + L.stage);
+    a.stage_pidx = reinterpret_cast<uint32_t *>(S + L.stage_pidx);
+    a.stage_rsid = reinterpret_cast<uint32_t *>(S + L.stage_rsid);
+    a.stage_rank = reinterpret_cast<uint32_t *>(S + L.stage_rank);
 
     for (uint32_t pass = 0; pass < pl->p.spp; ++pass) {
         for (uint64_t w = 0; w < waves; ++w) {
@@ -997,6 +1089,7 @@ int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
             const unsigned full = (n + T - 1u) / T;
             const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<true>, (int)T, n);
             const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, (int)T, n);
+            const unsigned scatter_blocks = resident_blocks(ctx, (const void *)k_pt_bin_scatter<true>, (int)T, n);
             RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
             k_bt_raygen<<<full, T, 0, st>>>(bt, n_sc, base, n, pl->p.seed, sample_dev, pass, rays[0], pidx[0],
                                             rsid[0], psid, a.tput, a.rad, a.rng, &cnt[0], ray_counts);
@@ -1019,9 +1112,17 @@ int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
                 a.count_out = &cnt[d + 1];
                 a.scount = &scnt[d];
                 a.depth = d;
+                a.bins_out = cnt + kCntBins + 8u * (d + 1u);
                 k_pt_shade<true><<<shade_blocks, T, 0, st>>>(a);
                 ++k;
                 RT_CUDA_CTX(ctx, cudaGetLastError());
+                if (a.binning && d + 1u < pl->p.max_depth) {
+                    k_pt_bin_scatter<true><<<scatter_blocks, T, 0, st>>>(
+                        &cnt[d + 1], a.bins_out, a.stage, a.stage_pidx, a.stage_rsid, a.stage_rank, rays[q ^ 1u],
+                        pidx[q ^ 1u], rsid[q ^ 1u], n, ctx->d_err);
+                    ++k;
+                    RT_CUDA_CTX(ctx, cudaGetLastError());
+                }
                 rc = launch_queue_trace_multi(ctx, st, views, n_sc, a.ssid, a.srays, nullptr, socc, &scnt[d], n,
                                               &tcnt[2 * d + 1], true, shape);
                 if (rc) return rc;
@@ -1079,8 +1180,10 @@ extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene 
     *plan = nullptr;
     if (flags & ~(RT_BATCH_GRAPH | RT_BATCH_DISCARD))
         return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: unknown flags");
-    if (p->max_depth == 0 || p->max_depth > kMaxPtDepth || p->spp == 0 || p->flags || p->reserved)
-        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_batch_plan_create: spp >= 1, max_depth in 1..64, flags 0");
+    if (p->max_depth == 0 || p->max_depth > kMaxPtDepth || p->spp == 0 || (p->flags & ~RT_PT_OCTANT_BINNING) ||
+        p->reserved)
+        return set_error(ctx, RT_ERR_INVALID_ARG,
+                         "rt_batch_plan_create: spp >= 1, max_depth in 1..64, flags 0 or RT_PT_OCTANT_BINNING");
     uint64_t P = 0, NL = 0;
     const char *why = nullptr;
     int rc = batch_totals(scenes, n_scenes, &P, &NL, &why);
@@ -1140,14 +1243,17 @@ extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene 
     // Load every kernel the launches use (and size the grid-stride grids)
     // before a capture begins, so that nothing is loaded while capturing.
     {
-        const void *kernels[] = {(const void *)k_bt_setup, (const void *)k_bt_raygen, (const void *)k_bt_accumulate,
-                                 (const void *)k_bt_sample, (const void *)k_pt_shade<true>, (const void *)k_pt_resolve};
+        const void *kernels[] = {(const void *)k_bt_setup,       (const void *)k_bt_raygen,
+                                 (const void *)k_bt_accumulate,  (const void *)k_bt_sample,
+                                 (const void *)k_pt_shade<true>, (const void *)k_pt_resolve,
+                                 (const void *)k_pt_bin_scatter<true>};
         cudaFuncAttributes fa;
         for (const void *k : kernels)
             if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
         if (e == cudaSuccess) {
             resident_blocks(ctx, (const void *)k_pt_shade<true>, (int)tt.shade_threads, 1u);
             resident_blocks(ctx, (const void *)k_pt_resolve, (int)tt.shade_threads, 1u);
+            resident_blocks(ctx, (const void *)k_pt_bin_scatter<true>, (int)tt.shade_threads, 1u);
             const TraceShape shape{tt.trace_threads, tt.trace_blocks_per_sm, tt.stack_ring, tt.refill};
             rc = prepare_queue_trace_multi(ctx, shape);
             if (rc) {
@@ -1182,7 +1288,8 @@ extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene 
     } else {
         // count the launches of one direct enqueue without issuing it
         const uint64_t waves = P ? (P + cap - 1u) / cap : 0u;
-        pl->kernels = P ? (uint32_t)(2u + (uint64_t)p->spp * waves * (2u + 4u * p->max_depth)) : 0u;
+        const uint64_t per_wave = 2u + 4u * p->max_depth + ((p->flags & RT_PT_OCTANT_BINNING) ? p->max_depth - 1u : 0u);
+        pl->kernels = P ? (uint32_t)(2u + (uint64_t)p->spp * waves * per_wave) : 0u;
     }
     *plan = pl;
     return RT_OK;

@@ -37,6 +37,7 @@ STATUS_NAMES = {0: "RT_OK", -1: "RT_ERR_INVALID_ARG", -2: "RT_ERR_OOM", -3: "RT_
                 -4: "RT_ERR_TIMEOUT", -5: "RT_ERR_BOUNDS", -6: "RT_ERR_UNSUPPORTED",
                 -7: "RT_ERR_NO_DEVICE", -8: "RT_ERR_NOT_FOUND"}
 RT_BUILD_WIDTH_MASK = 0xF << 16
+RT_PT_OCTANT_BINNING = 1
 RT_BATCH_GRAPH = 1
 RT_BATCH_DISCARD = 2
 RT_TUNE_FORCE = 1

@@ -40,7 +40,7 @@ typedef struct rt_batch_params {
     uint32_t spp;             /* samples per pixel per launch               */
     uint32_t max_depth;       /* path vertices, 1..64                        */
     uint32_t rr_depth;        /* Russian roulette from this vertex on        */
-    uint32_t flags;           /* 0                                           */
+    uint32_t flags;           /* 0 or RT_PT_OCTANT_BINNING (rtcore_pt.h)     */
     uint64_t seed;
     float ray_eps;
     uint32_t reserved;        /* 0                                           */

@@ -49,8 +49,18 @@ typedef struct rt_pt_params {
     uint32_t rr_depth;       /* Russian roulette from this vertex index on   */
     uint64_t seed;
     float ray_eps;           /* secondary-ray offset along the normal        */
-    uint32_t flags;          /* 0                                            */
+    uint32_t flags;          /* 0 or RT_PT_OCTANT_BINNING                    */
 } rt_pt_params;
+
+/* Traces the bounce rays of each path vertex grouped by direction octant (the
+ * shading kernel ranks each ray within its octant with one warp-level match
+ * and one atomic per octant present in the warp; a scatter pass places the
+ * octants one after the other), so the lanes of a traversal warp share a
+ * child visiting order.  The images do not depend on the order.  Off by
+ * default: on the GB300 the rays' spatial order (pixel order) is worth more
+ * to the traversal than their directional order -- 2M-triangle box at
+ * 1920x1080: 9.29 ms per sample in shading order, 9.51 ms binned. */
+#define RT_PT_OCTANT_BINNING 1u
 
 /* Scratch bytes of rt_path_trace for these parameters. */
 rt_status rt_pt_scratch_bytes(const rt_pt_params *p, uint64_t *bytes);

@@ -40,11 +40,11 @@ def test_scratch_sizing_and_validation(rtlib):
     rc, full = _scratch_bytes(rtlib, scenes)
     assert rc == rtcore.RT_OK
     paths = 512 * 512 + 700
-    assert paths * 197 <= full < paths * 197 + 64 * 1024  # 197 bytes of queues and path state per path
+    assert paths * 241 <= full < paths * 241 + 64 * 1024  # 241 bytes of queues and path state per path
     t = rtcore.default_batch_tuning()
     t.wave_paths = 4096
     rc, small = _scratch_bytes(rtlib, scenes, t)
-    assert rc == rtcore.RT_OK and 4096 * 197 <= small < full
+    assert rc == rtcore.RT_OK and 4096 * 241 <= small < full
     t.wave_paths = 10 ** 9  # larger than the batch: one wave
     assert _scratch_bytes(rtlib, scenes, t) == (rtcore.RT_OK, full)
     for field, value in (("stack_ring", 12), ("trace_threads", 64), ("refill", 33), ("shade_threads", 1024),

@@ -173,3 +173,23 @@ def test_batch_argument_errors(ctx, mid_scenes):
     assert e.value.code == rtcore.RT_ERR_INVALID_ARG
     with pytest.raises(rtcore.RtError):
         ctx.batch_plan(table, batch_params(1, 0, SEED), scratch, nb)
+
+
+def test_batch_with_octant_binning_gives_the_same_images(ctx, mid_scenes):
+    import rtcore
+    import torch
+    from rtcore.batch import batch_params
+    base, _ = _plan_run(ctx, mid_scenes, 2)
+    p = batch_params(2, 8, SEED)
+    p.flags = rtcore.RT_PT_OCTANT_BINNING
+    for sc in mid_scenes:
+        sc.accum.zero_()
+    table = [sc.batch_scene() for sc in mid_scenes]
+    nb = ctx.batch_scratch_bytes(table, p)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    plan = ctx.batch_plan(table, p, scratch, nb)
+    plan.launch(0)
+    ctx.sync()
+    plan.close()
+    for sc, b in zip(mid_scenes, base):
+        assert host(sc.accum).tobytes() == b.tobytes()

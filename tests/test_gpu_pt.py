@@ -71,3 +71,21 @@ def test_progressive_and_depth_limits(ctx, orc):
         g, _ = _run(ctx, sc, _params(w, h, 2, depth=depth, rr=rr))
         o = orc.path_trace(ob, tm, m, lights, S.BOX_CAMERA, w, h, 2, depth, rr, 0x5EED0003, 1e-4)
         assert host(g).view(np.float32).tobytes() == o.tobytes(), (depth, rr)
+
+
+def test_octant_binning_does_not_change_images(ctx, orc):
+    """Bounce rays traced in shading order (the default) or grouped by
+    direction octant (RT_PT_OCTANT_BINNING): the same image bit for bit, and
+    the oracle's."""
+    import rtcore
+    import rtcore.scenes as S
+    (v, i, tm, m, lights), blas, sc, keep = _scene(ctx, 10, 12)
+    w, h = 96, 72
+    binned, _ = _run(ctx, sc, _params(w, h, 3))
+    p = _params(w, h, 3)
+    p.flags = rtcore.RT_PT_OCTANT_BINNING
+    plain, _ = _run(ctx, sc, p)
+    assert host(binned).tobytes() == host(plain).tobytes()
+    ob, _ = orc.build_blas([(v, i, None)])
+    o = orc.path_trace(ob, tm, m, lights, S.BOX_CAMERA, w, h, 3, 8, 3, 0x5EED0003, 1e-4)
+    assert host(binned).view(np.float32).tobytes() == o.tobytes()
