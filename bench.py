@@ -355,16 +355,17 @@ def run_ours(args) -> int:
     # ---- e2e: rays from pinned host memory, hits back to host
     hp_rays = torch.from_numpy(prim.view(np.uint8)).pin_memory()
     hi_rays = torch.from_numpy(inc.view(np.uint8)).pin_memory()
-    hp_hits = torch.empty(n_p * 16, dtype=torch.uint8).pin_memory()
-    hi_hits = torch.empty(n_i * 16, dtype=torch.uint8).pin_memory()
+
+    # rt_trace_closest_host: the step's rays (primary, then incoherent) in and
+    # its hits out of pinned host memory, in chunks whose copies overlap the
+    # traversal of their neighbours
+    h_rays = torch.cat([hp_rays, hi_rays]).pin_memory()
+    h_hits = torch.empty(n_all * 16, dtype=torch.uint8).pin_memory()
+    hnb = ctx.trace_host_scratch_bytes(n_all)
+    hscratch = torch.empty(hnb, dtype=torch.uint8, device=dev)
 
     def e2e_step():
-        rays_p.copy_(hp_rays, non_blocking=True)
-        rays_i.copy_(hi_rays, non_blocking=True)
-        ctx.trace_closest(addr, rays_p, hits_p, n_p, stream=stream)
-        ctx.trace_closest(addr, rays_i, hits_i, n_i, stream=stream)
-        hp_hits.copy_(hits_p, non_blocking=True)
-        hi_hits.copy_(hits_i, non_blocking=True)
+        ctx.trace_closest_host(addr, h_rays, h_hits, n_all, hscratch, hnb, stream)
 
     for _ in range(2):
         e2e_step()

@@ -94,6 +94,17 @@ extern "C" rt_status rt_context_create(int device, rt_context **out) {
 extern "C" rt_status rt_context_destroy(rt_context *ctx) {
     if (!ctx) return RT_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
+    if (ctx->host_ready) {
+        cudaStreamSynchronize(ctx->h2d);
+        cudaStreamSynchronize(ctx->d2h);
+        for (int s = 0; s < rt_context::kHostSlots; ++s) {
+            cudaEventDestroy(ctx->ev_loaded[s]);
+            cudaEventDestroy(ctx->ev_traced[s]);
+            cudaEventDestroy(ctx->ev_free[s]);
+        }
+        cudaStreamDestroy(ctx->h2d);
+        cudaStreamDestroy(ctx->d2h);
+    }
     if (ctx->d_err) cudaFree(ctx->d_err);
     delete ctx;
     return RT_OK;

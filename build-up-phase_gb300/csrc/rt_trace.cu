@@ -447,6 +447,122 @@ extern "C" rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t ac
                         nullptr);
 }
 
+// ---------------------------------------------------------------------------
+// Rays and results in host memory: a ring of three device slots; chunk k is
+// copied in on the context's copy-in stream once its slot's previous results
+// have left, traced on the caller's stream, and copied out on the copy-out
+// stream, so the copies of neighbouring chunks overlap the traversal.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr uint32_t kHostChunk = 1u << 20;  // rays per chunk
+
+// The ring's geometry depends on the scratch size only (never on the call's
+// ray count or result size), so slot s covers the same bytes in every call
+// that passes the same scratch: its events then order all uses of it.
+struct HostSlots {
+    uint32_t chunk;  // rays per slot
+    uint64_t out_offset, slot_bytes;
+};
+
+uint64_t slot_bytes_for(uint32_t chunk) { return align_up((uint64_t)chunk * 32u, 256) + align_up((uint64_t)chunk * 16u, 256); }
+
+HostSlots host_slots(uint64_t scratch_bytes) {
+    HostSlots h;
+    h.slot_bytes = (scratch_bytes / (uint64_t)rt_context::kHostSlots) & ~255ull;
+    uint64_t c = h.slot_bytes / 48u;
+    if (c > kHostChunk) c = kHostChunk;
+    while (c > 0 && slot_bytes_for((uint32_t)c) > h.slot_bytes) --c;
+    h.chunk = (uint32_t)c;
+    h.out_offset = align_up(c * 32u, 256);
+    return h;
+}
+
+int host_setup(rt_context *ctx) {
+    if (ctx->host_ready) return RT_OK;
+    RT_CUDA_CTX(ctx, cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+    RT_CUDA_CTX(ctx, cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    for (int s = 0; s < rt_context::kHostSlots; ++s) {
+        RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_loaded[s], cudaEventDisableTiming));
+        RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_traced[s], cudaEventDisableTiming));
+        RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_free[s], cudaEventDisableTiming));
+    }
+    ctx->host_ready = true;
+    return RT_OK;
+}
+
+int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *hrays, void *hout, uint32_t n,
+               bool any, void *scratch, uint64_t scratch_bytes) {
+    if (n == 0) return RT_OK;
+    const HostSlots H = host_slots(scratch_bytes);
+    if (H.chunk == 0) return set_error(ctx, RT_ERR_OOM, "rt_trace_*_host: scratch smaller than rt_trace_host_scratch_bytes(1)");
+    if (reinterpret_cast<uintptr_t>(scratch) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_*_host: scratch must be 256-byte aligned");
+    RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+    int rc = host_setup(ctx);
+    if (rc) return rc;
+    if (scratch != ctx->host_scratch || scratch_bytes != ctx->host_scratch_bytes) {
+        // another ring: copy in nothing before every earlier copy out is done
+        for (int k = 0; k < rt_context::kHostSlots; ++k) RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_free[k], 0));
+        ctx->host_scratch = scratch;
+        ctx->host_scratch_bytes = scratch_bytes;
+    }
+    uint8_t *S = static_cast<uint8_t *>(scratch);
+    const uint32_t out_size = any ? 1u : 16u;
+    // at least four chunks per call (so that only a quarter of the copies
+    // fill and drain the pipeline), of 2^18 to 2^20 rays
+    uint32_t chunk = (uint32_t)align_up((n + 3u) / 4u, 1024);
+    if (chunk < kHostChunk / 4u) chunk = kHostChunk / 4u;
+    if (chunk > H.chunk) chunk = H.chunk;
+    int s = 0;
+    for (uint32_t off = 0; off < n; off += chunk) {
+        const uint32_t m = n - off < chunk ? n - off : chunk;
+        s = (int)(ctx->slot_next++ % (uint32_t)rt_context::kHostSlots);
+        uint8_t *rays_d = S + (uint64_t)s * H.slot_bytes;
+        uint8_t *out_d = rays_d + H.out_offset;
+        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_free[s], 0));
+        RT_CUDA_CTX(ctx, cudaMemcpyAsync(rays_d, hrays + off, (size_t)m * 32u, cudaMemcpyHostToDevice, ctx->h2d));
+        RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_loaded[s], ctx->h2d));
+        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(st, ctx->ev_loaded[s], 0));
+        rc = launch_batch(ctx, st, accel, reinterpret_cast<const rt_ray *>(rays_d),
+                          any ? nullptr : reinterpret_cast<rt_hit *>(out_d), nullptr, any ? out_d : nullptr, m, any,
+                          nullptr);
+        if (rc) return rc;
+        RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_traced[s], st));
+        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->d2h, ctx->ev_traced[s], 0));
+        RT_CUDA_CTX(ctx, cudaMemcpyAsync(static_cast<uint8_t *>(hout) + (size_t)off * out_size, out_d,
+                                         (size_t)m * out_size, cudaMemcpyDeviceToHost, ctx->d2h));
+        RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_free[s], ctx->d2h));
+    }
+    // the caller's stream goes on after the last results have left
+    RT_CUDA_CTX(ctx, cudaStreamWaitEvent(st, ctx->ev_free[s], 0));
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_trace_host_scratch_bytes(uint32_t n, int any_hit, uint64_t *bytes) {
+    (void)any_hit;  // one ring serves both kinds of call
+    if (!bytes) return RT_ERR_INVALID_ARG;
+    const uint32_t c = n == 0 ? 1u : (n < kHostChunk ? n : kHostChunk);
+    *bytes = slot_bytes_for(c) * (uint64_t)rt_context::kHostSlots;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_trace_closest_host(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                           rt_hit *hits, uint32_t n, void *scratch, uint64_t scratch_bytes) {
+    if (!ctx || !accel || (n && (!rays || !hits || !scratch)))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_closest_host: null argument");
+    return trace_host(ctx, static_cast<cudaStream_t>(stream), accel, rays, hits, n, false, scratch, scratch_bytes);
+}
+
+extern "C" rt_status rt_trace_any_host(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                       uint8_t *occluded, uint32_t n, void *scratch, uint64_t scratch_bytes) {
+    if (!ctx || !accel || (n && (!rays || !occluded || !scratch)))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_any_host: null argument");
+    return trace_host(ctx, static_cast<cudaStream_t>(stream), accel, rays, occluded, n, true, scratch, scratch_bytes);
+}
+
 extern "C" rt_status rt_trace_stats(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
                                     uint32_t n, int any_hit, unsigned long long *counters) {
     if (!ctx || !accel || !counters || (n && !rays)) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_stats: null argument");

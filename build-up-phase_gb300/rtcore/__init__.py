@@ -187,6 +187,9 @@ PROTOTYPES = {
     "rt_trace_closest": (_i32, [_vp, _vp, _u64, _vp, _vp, _vp, _u32]),
     "rt_trace_any": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32]),
     "rt_generate_primary_rays": (_i32, [_vp, _vp, C.POINTER(Camera), _u32, _u32, _f, _f, _vp]),
+    "rt_trace_host_scratch_bytes": (_i32, [_u32, _i32, C.POINTER(_u64)]),
+    "rt_trace_closest_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32, _vp, _u64]),
+    "rt_trace_any_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32, _vp, _u64]),
     "rt_trace_stats": (_i32, [_vp, _vp, _u64, _vp, _u32, _i32, _vp]),
     "rt_set_trace_tuning": (_i32, [_vp, C.POINTER(TraceTuning)]),
     "rt_get_trace_tuning": (_i32, [_vp, C.POINTER(TraceTuning)]),
@@ -341,6 +344,24 @@ class Context:
     def build_tlas(self, instances, n, flags, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
         self.check(self.lib.rt_build_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, flags, _ptr(accel),
                                           accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_tlas")
+
+    def trace_host_scratch_bytes(self, n: int, any_hit: bool = False) -> int:
+        out = C.c_uint64()
+        self.check(self.lib.rt_trace_host_scratch_bytes(n, 1 if any_hit else 0, C.byref(out)),
+                   "rt_trace_host_scratch_bytes")
+        return out.value
+
+    def trace_closest_host(self, accel_addr: int, rays, hits, n: int, scratch, scratch_bytes: int,
+                           stream=None) -> None:
+        """rays / hits: host buffers (torch CPU tensors, pinned for overlap, or
+        raw addresses)."""
+        self.check(self.lib.rt_trace_closest_host(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(hits), n,
+                                                  _ptr(scratch), scratch_bytes), "rt_trace_closest_host")
+
+    def trace_any_host(self, accel_addr: int, rays, occluded, n: int, scratch, scratch_bytes: int,
+                       stream=None) -> None:
+        self.check(self.lib.rt_trace_any_host(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(occluded), n,
+                                              _ptr(scratch), scratch_bytes), "rt_trace_any_host")
 
     def refit_blas(self, geoms, accel, accel_bytes, scratch, scratch_bytes, stream=None) -> None:
         arr = (GeometryTriangles * max(1, len(geoms)))(*geoms)

@@ -337,6 +337,26 @@ rt_status rt_trace_closest(rt_context *ctx, rt_stream stream, uint64_t accel,
 rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t accel,
                        const rt_ray *rays, uint8_t *occluded, uint32_t n);
 
+/*
+ * The same traversals with the rays and results in HOST memory (pinned for
+ * the copies to overlap): the rays go to the device and the results come
+ * back in chunks (a quarter of the call, 2^18 to 2^20 rays, at most what a
+ * slot holds) through a ring of three slots in
+ * `scratch` (rt_trace_host_scratch_bytes(n): enough for chunks of n rays; a
+ * smaller scratch means smaller chunks), the copies of neighbouring chunks
+ * running on the context's two copy streams while `stream` traces.  Calls that
+ * share a scratch buffer (closest and any hit alike) overlap each other's
+ * copies.  Asynchronous: the results are in host memory when `stream` reaches
+ * the end of the call.  The
+ * form a caller holding rays in host memory (the sample's CPU-side data, a
+ * plugin) uses in place of traceRayEXT batches (main.cpp:1047-1052).
+ */
+rt_status rt_trace_host_scratch_bytes(uint32_t n, int any_hit, uint64_t *bytes);
+rt_status rt_trace_closest_host(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                                rt_hit *hits, uint32_t n, void *scratch, uint64_t scratch_bytes);
+rt_status rt_trace_any_host(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,
+                            uint8_t *occluded, uint32_t n, void *scratch, uint64_t scratch_bytes);
+
 /* Pinhole primary rays of the sample's raygen (main.cpp:1036-1052) for a
  * width x height launch, written to a device array (row-major), tmin/tmax as
  * given.  Used to feed the batch API with the sample's camera model. */

@@ -265,6 +265,35 @@ def test_rt_sample_obj_mesh(rtlib, orc, tmp_path):
     assert (img[..., 2] != np.float32(0.2)).mean() > 0.5  # the box fills the view
 
 
+@pytest.mark.parametrize("n", [0, 1, 1000, (1 << 20) + 12345, 3 * (1 << 20) + 1])
+def test_host_memory_rays(ctx, orc, n):
+    """rt_trace_closest_host / rt_trace_any_host (rays and results in host
+    memory, chunked copies overlapping the traversal) give the device API's
+    results, from pinned and from pageable buffers, over repeated calls."""
+    import torch
+    import rtcore.scenes as S
+    items = soup(50_000, seed=3)
+    g = GpuBlas(ctx, items)
+    rays = S.incoherent_rays(77, max(n, 1), (0, 0, 0), (1, 1, 1), 1e30)[:n]
+    want = gpu_trace_closest(ctx, g.addr, rays) if n else np.zeros(0, np.uint8)
+    want_occ = gpu_trace_any(ctx, g.addr, rays) if n else np.zeros(0, np.uint8)
+    nb = max(ctx.trace_host_scratch_bytes(n), ctx.trace_host_scratch_bytes(n, True))
+    scratch = torch.empty(max(nb, 256), dtype=torch.uint8, device="cuda")
+    for pinned in (True, False):
+        hr = torch.from_numpy(rays.view(np.uint8).copy() if n else np.zeros(32, np.uint8))
+        hh = torch.full((max(n, 1) * 16,), 0xAB, dtype=torch.uint8)
+        ho = torch.full((max(n, 1),), 7, dtype=torch.uint8)
+        if pinned:
+            hr, hh, ho = hr.pin_memory(), hh.pin_memory(), ho.pin_memory()
+        for _ in range(2):
+            ctx.trace_closest_host(g.addr, hr, hh, n, scratch, nb)
+            ctx.trace_any_host(g.addr, hr, ho, n, scratch, nb)
+        ctx.sync()
+        if n:
+            assert hh.numpy()[:n * 16].tobytes() == want.tobytes()
+            assert ho.numpy()[:n].tobytes() == want_occ.tobytes()
+
+
 def test_full_size_soup_sampled(ctx, orc):
     """The 1M-triangle soup at full size: build bit-exact, and 2x2.07M rays
     traced on the GPU of which a seeded 40k sample is re-traced by the oracle
