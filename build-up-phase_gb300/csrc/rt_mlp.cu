@@ -383,16 +383,20 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
 // SBO = 16K (next 8-row group).  Thread 0 issues tcgen05.mma.kind::f16 with
 // M = 128, N = 64 (N = 16 for the output layer), K = 16 per instruction,
 // BF16 x BF16 -> FP32 accumulators in TMEM (row r = TMEM lane r), and commits
-// to an mbarrier.  The epilogue of every thread reads its row's 64
-// accumulators with tcgen05.ld (each warp its own 32-lane quarter), adds the
-// bias, applies ReLU, packs BF16 and writes the row into the next layer's
-// A tile; fence.proxy.async makes those generic-proxy stores visible to the
-// next MMA.  Every mbarrier wait is bounded: on expiry the kernel records
+// to an mbarrier.  The accumulators start from the layer's bias (written with
+// tcgen05.st), so the MMAs add the bias.  The epilogue of every thread reads
+// its row's 64 accumulators with tcgen05.ld (each warp its own 32-lane
+// quarter), applies ReLU and packs BF16 in one cvt.rn.relu.bf16x2.f32 per
+// pair, writes the row into the next layer's A tile and the next layer's bias
+// into the columns it has read; fence.proxy.async makes the generic-proxy
+// stores visible to the next MMA.  Every mbarrier wait is bounded: on expiry the kernel records
 // RT_ERR_TIMEOUT, waits once more (bounded) for its MMAs, frees its TMEM and
 // returns.
 
 constexpr int kTcRows = 128;
-constexpr uint32_t kTcTmemCols = 128;
+constexpr int kTcGroups = 4;                      // independent 128-row tile groups per CTA
+constexpr int kTcThreads = 128 * kTcGroups;
+constexpr uint32_t kTcTmemCols = 64u * kTcGroups;  // one 64-column accumulator per group
 // tile byte sizes / offsets
 __host__ __device__ constexpr uint32_t tc_tile_bytes(int rows, int k) { return (uint32_t)(rows / 8) * 16u * k; }
 __host__ __device__ constexpr uint32_t tc_w_off(int l) {
@@ -400,13 +404,18 @@ __host__ __device__ constexpr uint32_t tc_w_off(int l) {
     for (int i = 0; i < l; ++i) o += tc_tile_bytes(i == 5 ? 16 : 64, in_dim(i));
     return o;
 }
-constexpr uint32_t kTcWBytes = tc_w_off(6);                       // 47104
-constexpr uint32_t kTcA0 = kTcWBytes;                             // input tile, K = 96
-constexpr uint32_t kTcH0 = kTcA0 + tc_tile_bytes(kTcRows, 96);    // hidden tiles, K = 64
-constexpr uint32_t kTcH1 = kTcH0 + tc_tile_bytes(kTcRows, 64);
-constexpr uint32_t kTcBias = kTcH1 + tc_tile_bytes(kTcRows, 64);  // 336 floats
-constexpr uint32_t kTcBar = kTcBias + 336u * 4u;                  // mbarrier (8 B) + TMEM address (4 B)
-constexpr uint32_t kTcSmem = kTcBar + 64u;
+constexpr uint32_t kTcWBytes = tc_w_off(6);                        // 47104: all weights, shared by the groups
+constexpr uint32_t kTcBias = kTcWBytes;                            // 336 floats
+constexpr uint32_t kTcBar = kTcBias + 336u * 4u;                   // one mbarrier per group + the TMEM address
+constexpr uint32_t kTcGroupBase = (kTcBar + 64u + 127u) & ~127u;
+// per group: the K = 96 input tile (reused as the second hidden tile once
+// layer 0 has read it) and the first hidden tile (K = 64)
+constexpr uint32_t kTcA0 = 0;
+constexpr uint32_t kTcH0 = tc_tile_bytes(kTcRows, 96);
+constexpr uint32_t kTcH1 = kTcA0;
+constexpr uint32_t kTcGroupBytes = kTcH0 + tc_tile_bytes(kTcRows, 64);  // 40960
+constexpr uint32_t kTcSmem = kTcGroupBase + kTcGroups * kTcGroupBytes;
+static_assert(kTcSmem <= 227u * 1024u, "shared memory of the inference kernel");
 constexpr int kTcSpinLimit = 1 << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -463,39 +472,74 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 16 consecutive accumulator columns of this thread's TMEM lane from a
+// 16-byte aligned shared-memory array (four 16-byte loads)
+__device__ __forceinline__ void tc_st16_smem(uint32_t taddr, const float *src) {
+    const float4 *p = reinterpret_cast<const float4 *>(src);
+    const float4 a = p[0], b = p[1], c = p[2], d = p[3];
+    const float v[16] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
+        "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
+        "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// max(lo, 0) and max(hi, 0) rounded to BF16 and packed (lo in the low half):
+// one cvt.rn.relu.bf16x2.f32
+__device__ __forceinline__ uint32_t relu_pack_bf16(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__global__ void __launch_bounds__(128, 2) k_cache_query_tc(const CacheState *S, const rt_cache_input *in, float4 *out,
-                                                            uint32_t n, const uint32_t *n_dev, uint32_t *err) {
+__device__ __forceinline__ void group_sync(int group) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(kTcRows) : "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_cache_query_tc(const CacheState *S, const rt_cache_input *in,
+                                                                  float4 *out, uint32_t n, const uint32_t *n_dev,
+                                                                  uint32_t *err) {
     if (n_dev) n = min(n, *n_dev);
     extern __shared__ __align__(16) uint8_t smem[];
     uint8_t *sW = smem;
     float *sB = reinterpret_cast<float *>(smem + kTcBias);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kTcBar);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcBar + 8);
-    __shared__ int s_fail;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcBar);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcBar + 8u * kTcGroups);
+    // per group: set by a thread whose barrier wait ran out, before the
+    // group's barrier, read by all the group's threads after it (so the whole
+    // group leaves its loop together)
+    __shared__ int s_gfail[kTcGroups];
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int group = tid / kTcRows, gtid = tid % kTcRows;
+    uint8_t *gsm = smem + kTcGroupBase + (uint32_t)group * kTcGroupBytes;
 
-    // ---- weights (canonical K-major) and biases into shared memory
+    // ---- weights (canonical K-major) and biases into shared memory, once
     for (int l = 0; l < kLayers; ++l) {
         const int kin = in_dim(l), nout = l == 5 ? 16 : 64, nreal = out_dim(l);
         const __nv_bfloat16 *gw = S->wbf + w_off(l);
         __nv_bfloat16 *dst = reinterpret_cast<__nv_bfloat16 *>(sW + tc_w_off(l));
-        for (int e = tid; e < nout * kin; e += 128) {
+        for (int e = tid; e < nout * kin; e += kTcThreads) {
             const int o = e / kin, i = e % kin;
             dst[tc_off(o, i, kin) / 2] = o < nreal ? gw[o * kin + i] : __float2bfloat16(0.0f);
         }
     }
-    for (int e = tid; e < 336; e += 128) {
+    for (int e = tid; e < 336; e += kTcThreads) {
         const int l = e < 320 ? e / 64 : 5, o = e < 320 ? e % 64 : e - 320;
         sB[e] = o < out_dim(l) ? S->params[b_off(l) + o] : 0.0f;
     }
+    if (tid < kTcGroups) s_gfail[tid] = 0;
     if (tid == 0) {
-        s_fail = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-        // make the initialised barrier visible to the tensor core's arrivals
+        for (int g = 0; g < kTcGroups; ++g)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + g)) : "memory");
+        // make the initialised barriers visible to the tensor core's arrivals
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -508,92 +552,123 @@ __global__ void __launch_bounds__(128, 2) k_cache_query_tc(const CacheState *S, 
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    const uint32_t bar_a = smem_u32(bar);
+    // this group's accumulator columns; warp w of the group reads TMEM lanes
+    // [32 (w % 4), 32 (w % 4) + 32)
+    const uint32_t tmem = *tmem_slot + 64u * (uint32_t)group;
+    const uint32_t bar_a = smem_u32(bars + group);
     const uint32_t w_base = smem_u32(sW);
     uint32_t phase = 0;
+    volatile int *gfail = s_gfail + group;
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
 
-    for (uint32_t tile = blockIdx.x; tile < tiles && !s_fail; tile += gridDim.x) {
+    // The groups run independently (own tiles, buffers, barrier, phase): the
+    // tensor core works on one group's layer while the others encode or run
+    // their epilogues.
+    // this thread's input row of the group's next tile, loaded one tile ahead
+    const uint32_t tile_stride = gridDim.x * kTcGroups;
+    uint32_t tile = blockIdx.x * kTcGroups + (uint32_t)group;
+    rt_cache_input cur;
+    if (tile < tiles && tile * kTcRows + (uint32_t)gtid < n) cur = in[tile * kTcRows + (uint32_t)gtid];
+    for (; tile < tiles; tile += tile_stride) {
         // ---- encode this thread's row into the K = 96 input tile
-        const uint32_t row = tile * kTcRows + (uint32_t)tid;
+        const uint32_t row = tile * kTcRows + (uint32_t)gtid;
         {
             __align__(16) __nv_bfloat16 feat[96];
             if (row < n) {
-                encode_row(in[row], S, feat);
+                encode_row(cur, S, feat);
             } else {
                 for (int k = 0; k < 96; ++k) feat[k] = __float2bfloat16(0.0f);
             }
             for (int kc = 0; kc < 12; ++kc)
-                *reinterpret_cast<uint4 *>(smem + kTcA0 + tc_off(tid, 8 * kc, 96)) =
+                *reinterpret_cast<uint4 *>(gsm + kTcA0 + tc_off(gtid, 8 * kc, 96)) =
                     *reinterpret_cast<const uint4 *>(feat + 8 * kc);
+        }
+        // layer 0's bias into this row's accumulators: the MMAs add onto it
+        for (int c16 = 0; c16 < 4; ++c16) tc_st16_smem(tmem + lane_base + 16u * c16, sB + 16 * c16);
+        tc_wait_st();
+        {
+            const uint32_t nrow = (tile + tile_stride) * kTcRows + (uint32_t)gtid;
+            if (tile + tile_stride < tiles && nrow < n) cur = in[nrow];  // in flight during the layers
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(group);
         tc_fence_after();
 #pragma unroll 1
         for (int l = 0; l < kLayers; ++l) {
             const int kin = in_dim(l);
-            const uint32_t a_base = smem_u32(smem + (l == 0 ? kTcA0 : ((l & 1) ? kTcH0 : kTcH1)));
+            const uint32_t a_base = smem_u32(gsm + (l == 0 ? kTcA0 : ((l & 1) ? kTcH0 : kTcH1)));
             const uint32_t b_base = w_base + tc_w_off(l);
-            if (tid == 0) {
+            // the issuing thread alone waits for the MMAs; the rest of the
+            // group sleeps in the group barrier instead of polling
+            if (gtid == 0) {
                 const uint32_t idesc = tc_idesc(kTcRows, l == 5 ? 16 : 64);
                 for (int ks = 0; ks < kin / 16; ++ks) {
                     const uint64_t da = tc_desc(a_base + 256u * ks, 128u, 16u * kin);
                     const uint64_t db = tc_desc(b_base + 256u * ks, 128u, 16u * kin);
-                    tc_mma(tmem, da, db, idesc, ks > 0 ? 1u : 0u);
+                    tc_mma(tmem, da, db, idesc, 1u);  // onto the bias
                 }
                 tc_commit(bar_a);
-            }
-            const bool ok = mbar_wait_bounded(bar_a, phase);
-            phase ^= 1u;
-            if (!ok) {
-                report_error(err, RT_ERR_TIMEOUT, 0x90000000u | (uint32_t)l);
-                atomicExch(&s_fail, 1);
-            }
-            tc_fence_after();
-            if (l < 5) {
-                // hidden layer: bias + ReLU -> BF16 row of the next A tile
-                uint8_t *next = smem + ((l & 1) ? kTcH1 : kTcH0);
-                const float *bias = sB + 64 * l;
-#pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    float v[16];
-                    tc_ld16(tmem + lane_base + 16u * c16, v);
-                    tc_wait_ld();
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int k = 0; k < 8; ++k)
-                        packed[k] = pack_bf16(fmaxf(v[2 * k] + bias[16 * c16 + 2 * k], 0.0f),
-                                              fmaxf(v[2 * k + 1] + bias[16 * c16 + 2 * k + 1], 0.0f));
-                    *reinterpret_cast<uint4 *>(next + tc_off(tid, 16 * c16, 64)) =
-                        make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    *reinterpret_cast<uint4 *>(next + tc_off(tid, 16 * c16 + 8, 64)) =
-                        make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                if (!mbar_wait_bounded(bar_a, phase)) {
+                    report_error(err, RT_ERR_TIMEOUT, 0x90000000u | (uint32_t)l);
+                    mbar_wait_bounded(bar_a, phase);  // once more: no MMA may outlive the TMEM
+                    *gfail = 1;
                 }
+                tc_fence_before();
+            }
+            phase ^= 1u;
+            group_sync(group);
+            tc_fence_after();
+            if (*gfail) break;  // read after the barrier: the same for the whole group
+            if (l < 5) {
+                // hidden layer: ReLU -> BF16 row of the next A tile; the
+                // next layer's bias replaces each column group once read
+                uint8_t *next = gsm + ((l & 1) ? kTcH1 : kTcH0);
+                const float *nbias = sB + 64 * (l + 1);
+#pragma unroll
+                for (int c32 = 0; c32 < 2; ++c32) {
+                    // two 16-column loads in flight per wait
+                    float v[2][16];
+                    tc_ld16(tmem + lane_base + 32u * c32, v[0]);
+                    tc_ld16(tmem + lane_base + 32u * c32 + 16u, v[1]);
+                    tc_wait_ld();
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int c16 = 2 * c32 + h;
+                        if (l < 4 || c16 == 0) tc_st16_smem(tmem + lane_base + 16u * c16, nbias + 16 * c16);
+                        uint32_t packed[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) packed[k] = relu_pack_bf16(v[h][2 * k], v[h][2 * k + 1]);
+                        *reinterpret_cast<uint4 *>(next + tc_off(gtid, 16 * c16, 64)) =
+                            make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                        *reinterpret_cast<uint4 *>(next + tc_off(gtid, 16 * c16 + 8, 64)) =
+                            make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    }
+                }
+                tc_wait_st();
             } else {
                 float v[16];
                 tc_ld16(tmem + lane_base, v);
                 tc_wait_ld();
-                if (row < n) out[row] = make_float4(v[0] + sB[320], v[1] + sB[321], v[2] + sB[322], 0.0f);
+                if (row < n) out[row] = make_float4(v[0], v[1], v[2], 0.0f);
             }
             fence_async_smem();
             tc_fence_before();
-            __syncthreads();
+            group_sync(group);
             tc_fence_after();
-            if (s_fail) break;
+            if (*gfail) break;
         }
+        if (*gfail) break;
     }
-    // ---- teardown: no MMA may still be running when TMEM is freed
-    __syncthreads();
-    if (s_fail && tid == 0) mbar_wait_bounded(bar_a, phase);
+    // ---- teardown: every MMA has been waited for (a group that gave up
+    // waited once more); free the TMEM
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tmem_slot), "r"(kTcTmemCols)
+                     : "memory");
 }
 
 __global__ void k_cache_adam(CacheState *S) {
@@ -712,10 +787,10 @@ extern "C" rt_status rt_cache_query(rt_context *ctx, rt_stream stream, const voi
     if (n == 0) return RT_OK;
     int rc = set_smem(ctx);
     if (rc) return rc;
-    const uint32_t tiles = (n + kQueryRows - 1) / kQueryRows;
-    uint32_t grid = (uint32_t)ctx->sm_count * 2u;
-    if (grid > tiles) grid = tiles;
-    k_cache_query_tc<<<grid, 128, kTcSmem, static_cast<cudaStream_t>(stream)>>>(
+    const uint32_t groups = (n + kQueryRows * kTcGroups - 1) / (kQueryRows * kTcGroups);
+    uint32_t grid = (uint32_t)ctx->sm_count;
+    if (grid > groups) grid = groups;
+    k_cache_query_tc<<<grid, kTcThreads, kTcSmem, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const CacheState *>(cache), in, reinterpret_cast<float4 *>(out), n, nullptr, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
@@ -861,10 +936,10 @@ int cache_query_dev(rt_context *ctx, cudaStream_t st, const void *cache, const r
     if (max_n == 0) return RT_OK;
     int rc = set_smem(ctx);
     if (rc) return rc;
-    const uint32_t tiles = (max_n + kQueryRows - 1) / kQueryRows;
-    uint32_t grid = (uint32_t)ctx->sm_count * 2u;
-    if (grid > tiles) grid = tiles;
-    k_cache_query_tc<<<grid, 128, kTcSmem, st>>>(static_cast<const CacheState *>(cache), in,
+    const uint32_t groups = (max_n + kQueryRows * kTcGroups - 1) / (kQueryRows * kTcGroups);
+    uint32_t grid = (uint32_t)ctx->sm_count;
+    if (grid > groups) grid = groups;
+    k_cache_query_tc<<<grid, kTcThreads, kTcSmem, st>>>(static_cast<const CacheState *>(cache), in,
                                                  reinterpret_cast<float4 *>(out), max_n, n_dev, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
