@@ -178,6 +178,20 @@ def cpu_trace_rate(v, i, prim, inc, n_sample: int, threads: int = 0, repeats: in
     return len(rays) / min(times) / 1e6, len(rays), (threads or oracle.hw_threads())
 
 
+def whole_job(ms_step: float, units_per_rank: int, world: int, device=None):
+    """(step time, whole-job M units/s): the slowest rank's step time (max over
+    ranks through torch.distributed when `device` is given -- the replicas
+    each trace the full workload, no data-path collective) and the units all
+    ranks processed per second at that time."""
+    if device is not None and world > 1:
+        import torch
+        import torch.distributed as tdist
+        t = torch.tensor([ms_step], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    return ms_step, units_per_rank * world / (ms_step * 1e-3) / 1e6
+
+
 def run_reference(args) -> int:
     rank = _env_int("RANK", 0)
     if rank != 0:
@@ -309,11 +323,7 @@ def run_ours(args) -> int:
     t_p = [e[0].elapsed_time(e[1]) for e in evs]
     t_i = [e[1].elapsed_time(e[2]) for e in evs]
     ms_step = (sum(t_p) + sum(t_i)) / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = n_all * world / (ms_step * 1e-3) / 1e6
+    ms_step, value = whole_job(ms_step, n_all, world, dev if dist else None)
 
     # ---- roofline of the traversal kernel (both launches of the step)
     peaks = _peaks()
