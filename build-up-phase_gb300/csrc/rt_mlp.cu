@@ -9,16 +9,16 @@
 //   layer 5: 64 -> 8 (3 used), linear
 // Inference (queries): tcgen05 MMAs with TMEM accumulators, see
 // k_cache_query_tc.
-// Training forward: one warp owns 16 rows; each layer is m16n8k16 BF16 MMAs
-// with FP32 accumulation; the FP32 accumulator fragment of one layer is
-// exactly the A-operand fragment layout of the next (after bias, ReLU and
-// BF16 packing), so activations never leave registers between layers.
-// Weights sit in shared memory with padded row strides.
-// Backward (training): the same MMA routine propagates delta through W^T
-// (transposed into shared memory at block start); weight gradients are FP32
-// outer products on the CUDA cores over the 64-row tile, added to global
-// FP32 gradients with atomics; Adam updates the FP32 master copy and
-// refreshes the BF16 one.
+// Training forward: one warp owns 16 rows of a 128-row tile; each layer is
+// m16n8k16 BF16 MMAs with FP32 accumulation; the FP32 accumulator fragment of
+// one layer is exactly the A-operand fragment layout of the next (after bias,
+// ReLU and BF16 packing), so activations never leave registers between
+// layers.  Weights sit in shared memory with padded row strides.
+// Backward: the same MMAs propagate delta through W (B fragments of W read
+// transposed from its forward layout with ldmatrix.trans); the weight
+// gradients delta^T A are MMAs too (both operands loaded transposed with
+// ldmatrix.trans), added to global FP32 gradients once per weight and tile;
+// Adam updates the FP32 master copy and refreshes the BF16 one.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -49,18 +49,6 @@ static_assert(w_off(kLayers) == kParams, "parameter count");
 
 // shared-memory strides (elements): +8 bf16 keeps fragment loads conflict free
 __host__ __device__ constexpr int w_stride(int l) { return in_dim(l) + 8; }
-constexpr int kWtStride = 72;    // W^T of a 64-output layer: [in][64 + 8]
-constexpr int kWt5Stride = 24;   // W^T of the 8-output layer: [64][16 + 8]
-__host__ __device__ constexpr int sw_off(int l) {
-    int o = 0;
-    for (int k = 0; k < l; ++k) o += out_dim(k) * w_stride(k);
-    return o;
-}
-constexpr int kSwElems = sw_off(kLayers);                      // 25664
-__host__ __device__ constexpr int swt_off(int l) {               // l = 1..5
-    return (l - 1) * 64 * kWtStride;
-}
-constexpr int kSwtElems = 4 * 64 * kWtStride + 64 * kWt5Stride;  // 19968
 constexpr int kBiasFloats = 64 * 5 + 8;
 constexpr int kInStride = 104;
 constexpr int kActStride = 72;
@@ -172,75 +160,156 @@ __device__ void encode_row(const rt_cache_input &in, const CacheState *S, __nv_b
         *reinterpret_cast<uint32_t *>(out + k) = pack_bf16(f[k], f[k + 1]);
 }
 
-// Loads the BF16 weights (row-major, padded strides) and FP32 biases into
-// shared memory; with transpose, also W^T of layers 1..5.
-__device__ void load_weights(const CacheState *S, __nv_bfloat16 *sW, __nv_bfloat16 *sWT, float *sB) {
+constexpr int kQueryRows = 128;
+
+// ---------------------------------------------------------------------------
+// Training: forward + backward over 128-row tiles, gradients into S->grads
+// ---------------------------------------------------------------------------
+//
+// Eight warps, 16 rows each.  Forward as in the inference form, keeping each
+// layer's BF16 post-activations.  Backward, layer L = 5 .. 0: the weight and
+// bias gradients dW_L = delta_L^T A_{L-1}, db_L = sum delta_L over the tile's
+// 128 rows, on the tensor cores (m16n8k16, BF16 operands loaded transposed
+// from shared memory with ldmatrix.trans, FP32 accumulation, one atomic add
+// per weight and tile), then delta_{L-1} = (delta_L W_L) * relu'(A_{L-1})
+// with W_L read transposed by ldmatrix.trans from its forward layout.
+
+constexpr int kTrainRows = 128;
+constexpr int kTrainThreads = 256;
+__host__ __device__ constexpr int tw_rows(int l) { return l == 5 ? 16 : 64; }  // weight rows kept in shared memory
+__host__ __device__ constexpr int tw_off(int l) {
+    int o = 0;
+    for (int k = 0; k < l; ++k) o += tw_rows(k) * w_stride(k);
+    return o;
+}
+constexpr int kTwElems = tw_off(kLayers);                    // 26240 BF16
+constexpr int kDStride = 72;                                 // BF16 delta rows
+constexpr size_t kTrainSmem = (size_t)kTwElems * 2 + (size_t)kBiasFloats * 4 + (size_t)kTrainRows * kInStride * 2 +
+                              (size_t)5 * kTrainRows * kActStride * 2 + (size_t)kTrainRows * kDStride * 2;
+static_assert(kTrainSmem <= 227u * 1024u, "shared memory of the training kernel");
+
+__device__ __forceinline__ void ldsm_x4_t(const void *p, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)));
+}
+__device__ __forceinline__ void ldsm_x2_t(const void *p, uint32_t &r0, uint32_t &r1) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];"
+                 : "=r"(r0), "=r"(r1)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)));
+}
+
+// Weights (BF16, padded rows; the 8-output layer padded to 16 zero rows) and
+// FP32 biases into shared memory, 16 bytes at a time.
+__device__ void load_weights_train(const CacheState *S, __nv_bfloat16 *sW, float *sB) {
     for (int l = 0; l < kLayers; ++l) {
-        const int in = in_dim(l), out = out_dim(l);
-        const __nv_bfloat16 *gw = S->wbf + w_off(l);
-        for (int e = threadIdx.x; e < out * in; e += blockDim.x) {
-            const int o = e / in, i = e % in;
-            sW[sw_off(l) + o * w_stride(l) + i] = gw[e];
-            if (sWT && l >= 1) {
-                const int st = (l == 5) ? kWt5Stride : kWtStride;
-                sWT[swt_off(l) + i * st + o] = gw[e];
-            }
+        const int in = in_dim(l), chunks = in / 8;
+        const uint4 *gw = reinterpret_cast<const uint4 *>(S->wbf + w_off(l));
+        for (int e = threadIdx.x; e < tw_rows(l) * chunks; e += blockDim.x) {
+            const int o = e / chunks, c = e % chunks;
+            const uint4 v = o < out_dim(l) ? gw[o * chunks + c] : make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(sW + tw_off(l) + o * w_stride(l) + 8 * c) = v;
         }
-        if (sWT && l == 5)  // zero the padded k columns 8..15 of W5^T
-            for (int e = threadIdx.x; e < 64 * 16; e += blockDim.x) {
-                const int i = e / 16, k = e % 16;
-                if (k >= 8) sWT[swt_off(5) + i * kWt5Stride + k] = __float2bfloat16(0.0f);
-            }
     }
     for (int l = 0; l < kLayers; ++l)
         for (int e = threadIdx.x; e < out_dim(l); e += blockDim.x) sB[(l < 5 ? 64 * l : 320) + e] = S->params[b_off(l) + e];
 }
 
-constexpr int kQueryRows = 128;
-
-// ---------------------------------------------------------------------------
-// Training: forward + backward over 64-row tiles, gradients into S->grads
-// ---------------------------------------------------------------------------
-
-constexpr int kTrainRows = 64;
-constexpr size_t kTrainSmem = (size_t)kSwElems * 2 + (size_t)kSwtElems * 2 + (size_t)kBiasFloats * 4 +
-                              (size_t)kTrainRows * kInStride * 2 + (size_t)5 * kTrainRows * kActStride * 2 +
-                              (size_t)kTrainRows * 64 * 4 + 64 * 4;
-
-// dW[o][i] += sum_r delta[r][o] * A[r][i] over the 64 rows; db[o] += sum_r
-// delta[r][o].  PER weights per thread (128 threads).
-template <int IN, int OUT>
-__device__ void accum_grads(const float *sD, const __nv_bfloat16 *sA, int as, float *gW, float *gb) {
-    constexpr int PER = IN * OUT / 128;
-    constexpr int TPO = IN / PER;  // threads per output row
-    const int t = threadIdx.x;
-    const int o = t / TPO, i0 = (t % TPO) * PER;
-    float acc[PER];
+// c[j] = A (16 x 16*KS, registers) * W (row-major [16*KS][*], shared memory,
+// read transposed): the backward product delta * W over NT n-tiles of 8.
+template <int KS, int NT>
+__device__ __forceinline__ void warp_dense_wt(const uint32_t (&a)[KS][4], const __nv_bfloat16 *W, int ws,
+                                              float (&c)[NT][4], int lane) {
+    static_assert(NT % 2 == 0, "n-tiles in pairs");
+    const int row = lane & 7, mat = lane >> 3;
 #pragma unroll
-    for (int k = 0; k < PER; ++k) acc[k] = 0.0f;
-    for (int r = 0; r < kTrainRows; ++r) {
-        const float d = sD[r * 64 + o];
-        const __nv_bfloat16 *ar = sA + r * as + i0;
+    for (int j = 0; j < NT; ++j) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.0f;
 #pragma unroll
-        for (int k = 0; k < PER; k += 2) {
-            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(ar + k);
-            acc[k] += d * __bfloat162float(v.x);
-            acc[k + 1] += d * __bfloat162float(v.y);
+    for (int ks = 0; ks < KS; ++ks) {
+#pragma unroll
+        for (int jp = 0; jp < NT / 2; ++jp) {
+            // matrices: (k 0-7, n 0-7), (k 8-15, n 0-7), (k 0-7, n 8-15), (k 8-15, n 8-15)
+            const __nv_bfloat16 *p = W + (16 * ks + 8 * (mat & 1) + row) * ws + 16 * jp + 8 * (mat >> 1);
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4_t(p, b0, b1, b2, b3);
+            mma_bf16(c[2 * jp], a[ks], b0, b1);
+            mma_bf16(c[2 * jp + 1], a[ks], b2, b3);
+        }
+    }
+}
+
+// dW[o][i] += sum_r delta[r][o] * A[r][i] over the tile's 128 rows for the
+// outputs [o0, o0 + 16) and NT n-tiles of inputs from i0, on the tensor
+// cores; rows o >= OUT (padding) are dropped.
+template <int IN, int OUT, int NT>
+__device__ __forceinline__ void warp_grad_w(const __nv_bfloat16 *sD, const __nv_bfloat16 *sA, int as, int o0, int i0,
+                                            float *gW, int lane) {
+    const int row = lane & 7, mat = lane >> 3, g = lane >> 2, q = lane & 3;
+    float c[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.0f;
+#pragma unroll 2
+    for (int ks = 0; ks < kTrainRows / 16; ++ks) {
+        const int r = 16 * ks;
+        // A = delta^T (m = output, k = row): matrices (rows r..r+7 | r+8..r+15) x (o0.. | o0+8..)
+        uint32_t a[4];
+        ldsm_x4_t(sD + (r + 8 * (mat >> 1) + row) * kDStride + o0 + 8 * (mat & 1), a[0], a[1], a[2], a[3]);
+        if constexpr (NT == 1) {
+            uint32_t b0, b1;
+            ldsm_x2_t(sA + (r + 8 * (mat & 1) + row) * as + i0, b0, b1);
+            mma_bf16(c[0], a, b0, b1);
+        } else {
+#pragma unroll
+            for (int jp = 0; jp < NT / 2; ++jp) {
+                // B = A (k = row, n = input): matrices (r.., i) (r+8.., i) (r.., i+8) (r+8.., i+8)
+                uint32_t b0, b1, b2, b3;
+                ldsm_x4_t(sA + (r + 8 * (mat & 1) + row) * as + i0 + 16 * jp + 8 * (mat >> 1), b0, b1, b2, b3);
+                mma_bf16(c[2 * jp], a, b0, b1);
+                mma_bf16(c[2 * jp + 1], a, b2, b3);
+            }
         }
     }
 #pragma unroll
-    for (int k = 0; k < PER; ++k)
-        if (acc[k] != 0.0f) atomicAdd(gW + o * IN + i0 + k, acc[k]);
+    for (int j = 0; j < NT; ++j) {
+        const int i = i0 + 8 * j + 2 * q;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int o = o0 + g + (e >= 2 ? 8 : 0);
+            if (o < OUT && c[j][e] != 0.0f) atomicAdd(gW + o * IN + i + (e & 1), c[j][e]);
+        }
+    }
+}
+
+// db[o] += sum_r delta[r][o] (threads o < OUT).
+template <int OUT>
+__device__ __forceinline__ void grad_b(const __nv_bfloat16 *sD, float *gb) {
+    const int t = threadIdx.x;
     if (t < OUT) {
         float s = 0.0f;
-        for (int r = 0; r < kTrainRows; ++r) s += sD[r * 64 + t];
+        for (int r = 0; r < kTrainRows; ++r) s += __bfloat162float(sD[r * kDStride + t]);
         if (s != 0.0f) atomicAdd(gb + t, s);
     }
 }
 
-__global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_cache_input *in,
-                                                       const float4 *targets, uint32_t n, float inv_count,
-                                                       const uint32_t *n_dev, uint32_t row0) {
+// The weight and bias gradients of layer L, split over the eight warps.
+__device__ __forceinline__ void grads_of_layer(int L, const __nv_bfloat16 *sD, const __nv_bfloat16 *ain, int as,
+                                               float *grads, int warp, int lane) {
+    if (L == 0) {
+        warp_grad_w<96, 64, 6>(sD, ain, as, 16 * (warp & 3), 48 * (warp >> 2), grads + w_off(0), lane);
+        grad_b<64>(sD, grads + b_off(0));
+    } else if (L == 5) {
+        warp_grad_w<64, 8, 1>(sD, ain, as, 0, 8 * warp, grads + w_off(5), lane);
+        grad_b<8>(sD, grads + b_off(5));
+    } else {
+        warp_grad_w<64, 64, 4>(sD, ain, as, 16 * (warp & 3), 32 * (warp >> 2), grads + w_off(L), lane);
+        grad_b<64>(sD, grads + b_off(L));
+    }
+}
+
+__global__ void __launch_bounds__(kTrainThreads, 1) k_cache_fwd_bwd(CacheState *S, const rt_cache_input *in,
+                                                                    const float4 *targets, uint32_t n,
+                                                                    float inv_count, const uint32_t *n_dev,
+                                                                    uint32_t row0) {
     if (n_dev) {
         // rows [row0, row0 + n) of a set whose size is produced on the device
         const uint32_t total = *n_dev;
@@ -252,12 +321,11 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
     }
     extern __shared__ __align__(16) uint8_t smem[];
     __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smem);
-    __nv_bfloat16 *sWT = sW + kSwElems;
-    float *sB = reinterpret_cast<float *>(sWT + kSwtElems);
+    float *sB = reinterpret_cast<float *>(sW + kTwElems);
     __nv_bfloat16 *sIn = reinterpret_cast<__nv_bfloat16 *>(sB + kBiasFloats);
     __nv_bfloat16 *sAct = sIn + kTrainRows * kInStride;
-    float *sD = reinterpret_cast<float *>(sAct + 5 * kTrainRows * kActStride);
-    load_weights(S, sW, sWT, sB);
+    __nv_bfloat16 *sD = sAct + 5 * kTrainRows * kActStride;
+    load_weights_train(S, sW, sB);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, q = lane & 3;
     const int r0 = warp * 16;
@@ -277,7 +345,7 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
         uint32_t a0[6][4];
         load_a<6>(sIn, kInStride, r0, lane, a0);
         float c[8][4];
-        warp_dense<6, 8>(a0, sW + sw_off(0), w_stride(0), sB, c, lane);
+        warp_dense<6, 8>(a0, sW + tw_off(0), w_stride(0), sB, c, lane);
         uint32_t a[4][4];
         relu_to_a(c, a);
 #pragma unroll 1
@@ -292,13 +360,14 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
                 *reinterpret_cast<uint32_t *>(act + (r0 + g + 8) * kActStride + 16 * qq + 8 + 2 * q) = a[qq][3];
             }
             if (l <= 4) {
-                warp_dense<4, 8>(a, sW + sw_off(l), w_stride(l), sB + 64 * l, c, lane);
+                warp_dense<4, 8>(a, sW + tw_off(l), w_stride(l), sB + 64 * l, c, lane);
                 relu_to_a(c, a);
             }
         }
         float y[1][4];
-        warp_dense<4, 1>(a, sW + sw_off(5), w_stride(5), sB + 320, y, lane);
-        // ---- loss gradient at the outputs (cols 0..2 of each row)
+        warp_dense<4, 1>(a, sW + tw_off(5), w_stride(5), sB + 320, y, lane);
+        // ---- loss gradient at the outputs (cols 0..2 of each row); delta_5
+        // as BF16 (cols 0..15, 3..15 zero)
         float dy[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -312,30 +381,31 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
                 dy[e] = 2.0f * diff / den * inv_count;
                 loss += diff * diff / den;
             }
-            sD[rr * 64 + col] = dy[e];
         }
         uint32_t ad[4][4];
         ad[0][0] = pack_bf16(dy[0], dy[1]);
         ad[0][1] = pack_bf16(dy[2], dy[3]);
         ad[0][2] = 0u;
         ad[0][3] = 0u;
+        *reinterpret_cast<uint32_t *>(sD + (r0 + g) * kDStride + 2 * q) = ad[0][0];
+        *reinterpret_cast<uint32_t *>(sD + (r0 + g + 8) * kDStride + 2 * q) = ad[0][1];
+        *reinterpret_cast<uint32_t *>(sD + (r0 + g) * kDStride + 8 + 2 * q) = 0u;
+        *reinterpret_cast<uint32_t *>(sD + (r0 + g + 8) * kDStride + 8 + 2 * q) = 0u;
         // ---- backward, layers 5 .. 0
 #pragma unroll 1
         for (int L = 5; L >= 0; --L) {
-            __syncthreads();  // delta_L complete in sD
+            __syncthreads();  // delta_L and every activation complete
             const __nv_bfloat16 *ain = L == 0 ? sIn : sAct + (L - 1) * kTrainRows * kActStride;
             const int as = L == 0 ? kInStride : kActStride;
-            if (L == 5) accum_grads<64, 8>(sD, ain, as, S->grads + w_off(5), S->grads + b_off(5));
-            else if (L == 0) accum_grads<96, 64>(sD, ain, as, S->grads + w_off(0), S->grads + b_off(0));
-            else accum_grads<64, 64>(sD, ain, as, S->grads + w_off(L), S->grads + b_off(L));
+            grads_of_layer(L, sD, ain, as, S->grads, warp, lane);
             if (L == 0) break;
             // delta_{L-1} = (delta_L W_L) * relu'(act_{L-1})
             float dc[8][4];
             if (L == 5) {
                 uint32_t a1[1][4] = {{ad[0][0], ad[0][1], ad[0][2], ad[0][3]}};
-                warp_dense<1, 8>(a1, sWT + swt_off(5), kWt5Stride, nullptr, dc, lane);
+                warp_dense_wt<1, 8>(a1, sW + tw_off(5), w_stride(5), dc, lane);
             } else {
-                warp_dense<4, 8>(ad, sWT + swt_off(L), kWtStride, nullptr, dc, lane);
+                warp_dense_wt<4, 8>(ad, sW + tw_off(L), w_stride(L), dc, lane);
             }
             const __nv_bfloat16 *act = sAct + (L - 1) * kTrainRows * kActStride;
 #pragma unroll
@@ -349,20 +419,20 @@ __global__ void __launch_bounds__(128) k_cache_fwd_bwd(CacheState *S, const rt_c
                 if (!(__bfloat162float(m1.x) > 0.0f)) dc[j][2] = 0.0f;
                 if (!(__bfloat162float(m1.y) > 0.0f)) dc[j][3] = 0.0f;
             }
-            __syncthreads();  // everyone is done reading delta_L
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                sD[(r0 + g) * 64 + 8 * j + 2 * q] = dc[j][0];
-                sD[(r0 + g) * 64 + 8 * j + 2 * q + 1] = dc[j][1];
-                sD[(r0 + g + 8) * 64 + 8 * j + 2 * q] = dc[j][2];
-                sD[(r0 + g + 8) * 64 + 8 * j + 2 * q + 1] = dc[j][3];
-            }
 #pragma unroll
             for (int qq = 0; qq < 4; ++qq) {
                 ad[qq][0] = pack_bf16(dc[2 * qq][0], dc[2 * qq][1]);
                 ad[qq][1] = pack_bf16(dc[2 * qq][2], dc[2 * qq][3]);
                 ad[qq][2] = pack_bf16(dc[2 * qq + 1][0], dc[2 * qq + 1][1]);
                 ad[qq][3] = pack_bf16(dc[2 * qq + 1][2], dc[2 * qq + 1][3]);
+            }
+            __syncthreads();  // every warp is done reading delta_L
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) {
+                *reinterpret_cast<uint32_t *>(sD + (r0 + g) * kDStride + 16 * qq + 2 * q) = ad[qq][0];
+                *reinterpret_cast<uint32_t *>(sD + (r0 + g + 8) * kDStride + 16 * qq + 2 * q) = ad[qq][1];
+                *reinterpret_cast<uint32_t *>(sD + (r0 + g) * kDStride + 16 * qq + 8 + 2 * q) = ad[qq][2];
+                *reinterpret_cast<uint32_t *>(sD + (r0 + g + 8) * kDStride + 16 * qq + 8 + 2 * q) = ad[qq][3];
             }
         }
     }
@@ -713,7 +783,7 @@ int launch_fwd_bwd(rt_context *ctx, cudaStream_t st, CacheState *S, const rt_cac
     uint32_t grid = (uint32_t)ctx->sm_count;
     if (grid > tiles) grid = tiles;
     if (grid == 0) return RT_OK;
-    k_cache_fwd_bwd<<<grid, 128, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(tg), n,
+    k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(tg), n,
                                                    1.0f / (3.0f * (float)n), nullptr, 0u);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
@@ -958,7 +1028,7 @@ int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cach
         const uint32_t tiles = (m + kTrainRows - 1) / kTrainRows;
         uint32_t grid = (uint32_t)ctx->sm_count;
         if (grid > tiles) grid = tiles;
-        k_cache_fwd_bwd<<<grid, 128, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(targets), m, 0.0f,
+        k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(targets), m, 0.0f,
                                                        n_dev, b);
         k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S);
         k_cache_step<<<1, 32, 0, st>>>(S, nullptr);

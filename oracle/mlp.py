@@ -3,7 +3,7 @@
 Same padded parameter layout, encoding, network, loss and Adam as
 rtcore_cache.h, evaluated in float64 with BF16 rounding applied at exactly
 the points where the GPU rounds (encoded inputs, weights, the activations fed
-to the next layer, the deltas fed to the backward MMA).  The GPU accumulates
+to the next layer, the deltas fed to the backward and weight-gradient MMAs).  The GPU accumulates
 in FP32 in an unspecified order, so results are compared with a tolerance.
 """
 from __future__ import annotations
@@ -97,8 +97,9 @@ def gradient(p: np.ndarray, inputs: np.ndarray, targets: np.ndarray, lo, hi, exa
     g = np.zeros(N_PARAMS, np.float64)
     for L in range(5, -1, -1):
         wo, bo = W_OFF[L]
-        g[wo:bo] = (d.T @ acts[L]).reshape(-1)
-        g[bo:bo + OUT[L]] = d.sum(axis=0)
+        dr = _round(d, exact)  # the weight-gradient MMAs take delta in BF16
+        g[wo:bo] = (dr.T @ acts[L]).reshape(-1)
+        g[bo:bo + OUT[L]] = dr.sum(axis=0)
         if L == 0:
             break
         w, _ = layers[L]
