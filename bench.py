@@ -51,6 +51,11 @@ WORKLOAD = "triangle soup 1M tris (unit cube, edges U(0.001,0.02)); 1920x1080 pr
 BYTES_RAY_IO = 48   # 32 B ray in + 16 B hit out
 BYTES_NODE = 80     # compressed BVH8 node
 BYTES_TRI = 36      # FP32 vertex triplet
+# LBVH build, algorithmic bytes per triangle: 48 read for bounds and
+# centroids (12 B indices + 36 B vertices), 12 written as Morton key + id,
+# 24 per sort pass (8 passes of 63-bit keys), 2 x 24 for the radix tree and
+# its refit, 80 / 8 for the BVH8 node share of one leaf-equivalent
+BYTES_BUILD_PER_TRI = 48 + 12 + 24 * 8 + 2 * 24 + 80 // 8
 # DRAM bytes (read + write) of one step's two traversal launches measured by
 # ncu (cold caches): 97.5 MB primary + 392.0 MB incoherent
 TRAFFIC_BYTES_PER_STEP = 489_500_000
@@ -417,6 +422,12 @@ def run_ours(args) -> int:
                              "incoherent_mrays": round(n_i * args.steps / (sum(t_i) * 1e-3) / 1e6, 2),
                              "shadow_anyhit_mrays": round(shadow_mrays, 2),
                              "build_ms": round(statistics.median(build_ms), 3),
+                             "build_roofline": {
+                                 "bytes_per_tri": BYTES_BUILD_PER_TRI,
+                                 "achieved_gbs": round(N_TRIS * BYTES_BUILD_PER_TRI / (statistics.median(build_ms) * 1e-3) / 1e9, 1),
+                                 "frac_of_hbm": round(N_TRIS * BYTES_BUILD_PER_TRI / (statistics.median(build_ms) * 1e-3) / 1e9
+                                                      / peaks["hbm_gbs"], 4),
+                                 "note": "latency-bound: 13 dependent kernels, the collapse a cooperative grid of level barriers"},
                              "wall_s_timed_region": round(t_wall, 3)},
                "secondary": extra,
                "clocks": clocks.summary()}

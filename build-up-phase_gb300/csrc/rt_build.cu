@@ -68,18 +68,18 @@ BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
     uint64_t ni = n > 0 ? n - 1 : 0;
     uint64_t cap = node_capacity_for(n);
     L.recs = take((uint64_t)n * rec_bytes);
-    L.boxes = take((uint64_t)n * 24u);
+    L.boxes = take((uint64_t)n * 32u);
     L.keys0 = take((uint64_t)n * 8u);
     L.keys1 = take((uint64_t)n * 8u);
     L.ids0 = take((uint64_t)n * 4u);
     L.ids1 = take((uint64_t)n * 4u);
     L.bin = take(ni * 16u);
     L.parent = take((ni + n) * 4u);
-    L.node_box = take(ni * 24u);
+    L.node_box = take(ni * 32u);
     L.node_cost = take(ni * 4u);
     L.leafable = take(ni);
     L.visit = take(ni * 4u);
-    L.leaf_box = take((uint64_t)n * 24u);
+    L.leaf_box = take((uint64_t)n * 32u);
     L.wq = take(cap * 4u);
     L.slots = take(cap * 32u);
     L.counts = take(cap * 4u);
@@ -101,17 +101,21 @@ uint64_t accel_bytes_for(uint32_t n, uint32_t rec_bytes, uint32_t table_entries)
 // Device helpers
 // ---------------------------------------------------------------------------
 
+// Boxes in scratch: 32 bytes each (lo xyz, 0, hi xyz, 0), one L2 sector,
+// moved as two 16-byte accesses; loads go through L2 (other blocks of the
+// same launch write them).
 __device__ __forceinline__ Box load_box(const float *b, uint32_t i) {
+    const float4 *p = reinterpret_cast<const float4 *>(b) + (size_t)i * 2u;
+    const float4 lo = __ldcg(p), hi = __ldcg(p + 1);
     Box x;
-    const float *p = b + (size_t)i * 6u;
-    x.lo[0] = __ldcg(p + 0); x.lo[1] = __ldcg(p + 1); x.lo[2] = __ldcg(p + 2);
-    x.hi[0] = __ldcg(p + 3); x.hi[1] = __ldcg(p + 4); x.hi[2] = __ldcg(p + 5);
+    x.lo[0] = lo.x; x.lo[1] = lo.y; x.lo[2] = lo.z;
+    x.hi[0] = hi.x; x.hi[1] = hi.y; x.hi[2] = hi.z;
     return x;
 }
 __device__ __forceinline__ void store_box(float *b, uint32_t i, const Box &x) {
-    float *p = b + (size_t)i * 6u;
-    p[0] = x.lo[0]; p[1] = x.lo[1]; p[2] = x.lo[2];
-    p[3] = x.hi[0]; p[4] = x.hi[1]; p[5] = x.hi[2];
+    float4 *p = reinterpret_cast<float4 *>(b) + (size_t)i * 2u;
+    p[0] = make_float4(x.lo[0], x.lo[1], x.lo[2], 0.0f);
+    p[1] = make_float4(x.hi[0], x.hi[1], x.hi[2], 0.0f);
 }
 
 __device__ __forceinline__ uint64_t spread3_21(uint32_t x) {
@@ -124,15 +128,29 @@ __device__ __forceinline__ uint64_t spread3_21(uint32_t x) {
     return v;
 }
 
-__device__ __forceinline__ void warp_minmax_atomic(int32_t *dst_min, int32_t *dst_max, int32_t mn, int32_t mx) {
+// Scene (centroid) bounds: per axis, the minimum and maximum of the
+// order-preserving integers of a 256-thread block (redux.sync within each
+// warp, shared memory across the eight warps), then one atomic per block and
+// value.  Called by every thread of the block.
+__device__ __forceinline__ void block_minmax_atomic(int32_t *cbounds, const int32_t (&mn)[3], const int32_t (&mx)[3]) {
+    __shared__ int32_t s_mm[8][6];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    for (int a = 0; a < 3; ++a) {
+        const int32_t wmn = __reduce_min_sync(0xffffffffu, mn[a]);
+        const int32_t wmx = __reduce_max_sync(0xffffffffu, mx[a]);
+        if (lane == 0) {
+            s_mm[warp][a] = wmn;
+            s_mm[warp][3 + a] = wmx;
+        }
     }
-    if ((threadIdx.x & 31) == 0) {
-        if (mn != INT32_MAX) atomicMin(dst_min, mn);
-        if (mx != INT32_MIN) atomicMax(dst_max, mx);
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int v = threadIdx.x;
+        int32_t r = s_mm[0][v];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = v < 3 ? min(r, s_mm[w][v]) : max(r, s_mm[w][v]);
+        if (v < 3 && r != INT32_MAX) atomicMin(cbounds + v, r);
+        if (v >= 3 && r != INT32_MIN) atomicMax(cbounds + v, r);
     }
 }
 
@@ -242,7 +260,7 @@ __global__ void __launch_bounds__(256) k_prep_tris(const GeomParams gp, uint32_t
                 cmax[a] = o;
             }
     }
-    for (int a = 0; a < 3; ++a) warp_minmax_atomic(&cbounds[a], &cbounds[3 + a], cmin[a], cmax[a]);
+    block_minmax_atomic(cbounds, cmin, cmax);
 }
 
 __device__ bool invert3x4(const float *m, float out[12]) {
@@ -312,7 +330,7 @@ __global__ void __launch_bounds__(256) k_prep_inst(const rt_instance *__restrict
                 cmax[a] = o;
             }
     }
-    for (int a = 0; a < 3; ++a) warp_minmax_atomic(&cbounds[a], &cbounds[3 + a], cmin[a], cmax[a]);
+    block_minmax_atomic(cbounds, cmin, cmax);
 }
 
 // ---------------------------------------------------------------------------
@@ -951,8 +969,8 @@ RefitLayout refit_layout(uint32_t n) {
     };
     const uint64_t cap = node_capacity_for(n);
     L.flag = take(16);
-    L.leaf_box = take((uint64_t)n * 24u);
-    L.node_box = take(cap * 24u);
+    L.leaf_box = take((uint64_t)n * 32u);
+    L.node_box = take(cap * 32u);
     L.parent = take(cap * 4u);
     L.arrive = take(cap * 4u);
     L.total = off;
@@ -1284,7 +1302,7 @@ extern "C" rt_status rt_debug_blas_scratch_layout(uint32_t n_tris, uint32_t flag
 namespace rtc {
 namespace {
 
-constexpr uint64_t kStaticScratchBytes = 32ull << 20;  // 32 MiB per device
+constexpr uint64_t kStaticScratchBytes = 40ull << 20;  // 40 MiB per device
 constexpr int kStaticScratchDevices = 64;
 
 __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];

@@ -254,7 +254,7 @@ rt_status rt_build_blas(rt_context *ctx, rt_stream stream,
  * counterpart in the reference (whose Vulkan sample allocates its scratch
  * buffer with vkAllocateMemory).
  *
- * The scratch is one fixed 32 MiB array compiled into the library, held in
+ * The scratch is one fixed 40 MiB array compiled into the library, held in
  * device memory of every GPU that loads the library until the process
  * exits; it limits a build to RT_STATIC_SCRATCH_MAX_TRIS triangles (larger
  * inputs return RT_ERR_UNSUPPORTED -- use rt_build_blas).  The first call on
@@ -290,7 +290,7 @@ rt_status rt_build_tlas(rt_context *ctx, rt_stream stream,
  * TLASes that reference it need a refit or a rebuild after it.  A structure
  * that does not match the inputs is left unchanged and RT_ERR_INVALID_ARG
  * surfaces at rt_sync.  scratch: rt_get_refit_scratch_bytes(primitives),
- * about 56 bytes per primitive.
+ * about 72 bytes per primitive.
  */
 rt_status rt_get_refit_scratch_bytes(uint32_t prim_count, uint64_t *bytes);
 rt_status rt_refit_blas(rt_context *ctx, rt_stream stream, const rt_geometry_triangles *geoms, uint32_t n_geoms,
