@@ -508,88 +508,151 @@ struct CollapseArgs {
 
 __device__ __forceinline__ bool ref_is_leaf(uint32_t r) { return (r & kLeafBit) != 0u; }
 __device__ __forceinline__ Box ref_box(const CollapseArgs &a, uint32_t r) {
-    return ref_is_leaf(r) ? load_box(a.leaf_box, r & ~kLeafBit) : load_box(a.node_box, r);
-}
-__device__ __forceinline__ bool ref_openable(const CollapseArgs &a, uint32_t r) {
-    return !ref_is_leaf(r) && a.leafable[r] == 0;
+    return load_box(ref_is_leaf(r) ? a.leaf_box : a.node_box, r & ~kLeafBit);
 }
 
-__device__ int collapse_children(const CollapseArgs &a, uint32_t src, uint32_t out[8]) {
-    if (!ref_openable(a, src)) { out[0] = src; return 1; }
-    uint4 nd = a.bin[src];
+// One child reference as the collapse sees it.  The box, the SAH leaf flag
+// and the binary node are independent loads (all written by earlier kernels
+// of the build, so read through the non-coherent path), issued together: the
+// greedy widening costs one round trip per opened node instead of one per
+// child and step.
+struct RefInfo {
+    uint32_t ref;
+    uint32_t kid0, kid1;  // binary children (internal references)
+    uint32_t cnt;         // primitives below; bit 31: internal and not a SAH leaf (gets widened)
+    float area;           // half surface area of the box
+};
+constexpr uint32_t kOpenBit = 0x80000000u;
+
+__device__ __forceinline__ Box load_box_ro(const CollapseArgs &a, uint32_t r) {
+    const float4 *p = reinterpret_cast<const float4 *>(ref_is_leaf(r) ? a.leaf_box : a.node_box) +
+                      (size_t)(r & ~kLeafBit) * 2u;
+    const float4 lo = __ldg(p), hi = __ldg(p + 1);
+    Box b;
+    b.lo[0] = lo.x; b.lo[1] = lo.y; b.lo[2] = lo.z;
+    b.hi[0] = hi.x; b.hi[1] = hi.y; b.hi[2] = hi.z;
+    return b;
+}
+
+__device__ __forceinline__ RefInfo fetch_ref(const CollapseArgs &a, uint32_t r) {
+    const bool leaf = ref_is_leaf(r);
+    const uint32_t i = r & ~kLeafBit;
+    const Box b = load_box_ro(a, r);
+    uint4 nd = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t lf = 1u;
+    if (!leaf) {
+        nd = __ldg(a.bin + i);
+        lf = __ldg(a.leafable + i);
+    }
+    RefInfo x;
+    x.ref = r;
+    x.kid0 = nd.x;
+    x.kid1 = nd.y;
+    x.cnt = (leaf ? 1u : nd.w - nd.z + 1u) | ((!leaf && lf == 0u) ? kOpenBit : 0u);
+    x.area = half_area(b);
+    return x;
+}
+__device__ __forceinline__ bool info_open(const RefInfo &x) { return (x.cnt & kOpenBit) != 0u; }
+
+// Greedy widening: while fewer than `width` children, open the openable
+// child of largest surface area (the first on ties).  Arrays are indexed by
+// unrolled compare-and-select so they stay in registers.
+__device__ __forceinline__ int collapse_children(const CollapseArgs &a, const RefInfo &src, RefInfo ch[8]) {
+    if (!info_open(src)) {
+        ch[0] = src;
+        return 1;
+    }
+    ch[0] = fetch_ref(a, src.kid0);
+    ch[1] = fetch_ref(a, src.kid1);
     int n = 2;
-    out[0] = nd.x;
-    out[1] = nd.y;
     while (n < (int)a.width) {
         int best = -1;
         float best_a = -1.0f;
-        for (int i = 0; i < n; ++i) {
-            if (!ref_openable(a, out[i])) continue;
-            float ar = half_area(ref_box(a, out[i]));
-            if (ar > best_a) { best_a = ar; best = i; }
-        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (i < n && info_open(ch[i]) && ch[i].area > best_a) { best_a = ch[i].area; best = i; }
         if (best < 0) break;
-        uint4 c = a.bin[out[best]];
-        out[best] = c.x;
-        out[n++] = c.y;
+        uint32_t k0 = 0u, k1 = 0u;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (i == best) { k0 = ch[i].kid0; k1 = ch[i].kid1; }
+        const RefInfo x0 = fetch_ref(a, k0), x1 = fetch_ref(a, k1);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (i == best) ch[i] = x0;
+            if (i == n) ch[i] = x1;
+        }
+        ++n;
     }
     return n;
 }
 
-__device__ void assign_slots(const Box &node, const Box *cb, int n, int slot_of[8]) {
-    float diff[8][3];
-    float ncen[3];
+// Octant slot of each child: repeatedly the (child, slot) pair of least
+// cost (x + y) + z, the centre offset signed by the slot's octant, the first
+// pair in (child, slot) order on ties.  The child boxes are reloaded here (L1
+// hits: the widening has just fetched them).  Returns the slot of child c in
+// bits 4c..4c+3.
+__device__ __forceinline__ uint32_t assign_slots(const CollapseArgs &a, uint32_t src, const RefInfo ch[8], int n) {
+    const Box node = load_box_ro(a, src);
     const bool ne = box_is_empty(node);
+    float ncen[3], diff[8][3];
+#pragma unroll
     for (int q = 0; q < 3; ++q) ncen[q] = (node.lo[q] + node.hi[q]) * 0.5f;
-    for (int c = 0; c < n; ++c)
-        for (int q = 0; q < 3; ++q)
-            diff[c][q] = (box_is_empty(cb[c]) || ne) ? 0.0f : (cb[c].lo[q] + cb[c].hi[q]) * 0.5f - ncen[q];
-    bool used[8] = {false, false, false, false, false, false, false, false};
-    for (int c = 0; c < n; ++c) slot_of[c] = -1;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        Box cb = box_empty();
+        if (c < n) cb = load_box_ro(a, ch[c].ref);
+        const bool ce = box_is_empty(cb);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) diff[c][q] = (ce || ne) ? 0.0f : (cb.lo[q] + cb.hi[q]) * 0.5f - ncen[q];
+    }
+    uint32_t used = 0u, done = 0u, code = 0u;
     for (int it = 0; it < n; ++it) {
         int bc = -1, bs = -1;
         float bv = kInf;
-        for (int c = 0; c < n; ++c) {
-            if (slot_of[c] >= 0) continue;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            if (c >= n || ((done >> c) & 1u)) continue;
+#pragma unroll
             for (int s = 0; s < 8; ++s) {
-                if (used[s]) continue;
-                float x = (s & 1) ? -diff[c][0] : diff[c][0];
-                float y = (s & 2) ? -diff[c][1] : diff[c][1];
-                float z = (s & 4) ? -diff[c][2] : diff[c][2];
-                float cost = (x + y) + z;
+                if ((used >> s) & 1u) continue;
+                const float x = (s & 1) ? -diff[c][0] : diff[c][0];
+                const float y = (s & 2) ? -diff[c][1] : diff[c][1];
+                const float z = (s & 4) ? -diff[c][2] : diff[c][2];
+                const float cost = (x + y) + z;
                 if (bc < 0 || cost < bv) { bc = c; bs = s; bv = cost; }
             }
         }
-        slot_of[bc] = bs;
-        used[bs] = true;
+        done |= 1u << bc;
+        used |= 1u << bs;
+        code |= (uint32_t)bs << (4 * bc);
     }
+    return code;
 }
 
 // Phase A: children and slots of wide node k; returns (n_int, n_prim).
 __device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, uint32_t &n_int, uint32_t &n_prim) {
     // wq, slots and counts are written by other blocks of this launch between
     // grid barriers: read them through L2 (__ldcg), never a stale L1 line.
-    uint32_t src = __ldcg(a.wq + k);
-    uint32_t ch[8];
-    int nc = collapse_children(a, src, ch);
-    Box cb[8];
-    for (int c = 0; c < nc; ++c) cb[c] = ref_box(a, ch[c]);
-    Box nbox = ref_box(a, src);
-    int slot_of[8];
-    assign_slots(nbox, cb, nc, slot_of);
+    const uint32_t sref = __ldcg(a.wq + k);
+    RefInfo ch[8];
+    const int nc = collapse_children(a, fetch_ref(a, sref), ch);
+    const uint32_t code = assign_slots(a, sref, ch, nc);
     uint32_t slot_ref[8] = {kNone, kNone, kNone, kNone, kNone, kNone, kNone, kNone};
-    for (int c = 0; c < nc; ++c) slot_ref[slot_of[c]] = ch[c];
     uint32_t ni = 0, np = 0;
-    for (int s = 0; s < 8; ++s) {
-        uint32_t r = slot_ref[s];
-        a.slots[(size_t)k * 8u + s] = r;
-        if (r == kNone) continue;
-        if (ref_openable(a, r)) {
-            ++ni;
-        } else {
-            np += ref_is_leaf(r) ? 1u : (a.bin[r].w - a.bin[r].z + 1u);
-        }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        if (c >= nc) continue;
+        const uint32_t s = (code >> (4 * c)) & 0xfu;
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if ((uint32_t)t == s) slot_ref[t] = ch[c].ref;
+        if (info_open(ch[c])) ++ni;
+        else np += ch[c].cnt;
     }
+    uint4 *o = reinterpret_cast<uint4 *>(a.slots + (size_t)k * 8u);
+    o[0] = make_uint4(slot_ref[0], slot_ref[1], slot_ref[2], slot_ref[3]);
+    o[1] = make_uint4(slot_ref[4], slot_ref[5], slot_ref[6], slot_ref[7]);
     n_int = ni;
     n_prim = np;
 }
@@ -639,48 +702,98 @@ __device__ __forceinline__ uint32_t pack_meta4(const uint8_t *b) {
     return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
 }
 
-// Phase B: writes wide node k with its child and record bases.
+// Leaf records of one wide node, gathered from input order into node order.
+// The first record of each leaf child is loaded G children at a time before
+// any is stored, so the loads overlap; the further primitives of collapsed
+// subtrees (at most RT_MAX_LEAF_PRIMS - 1 per child) follow.
+template <int RW, int G>
+__device__ __forceinline__ void copy_leaf_records(const CollapseArgs &a, const uint32_t leafc, const uint32_t id0[8],
+                                                  const uint32_t first[8], const uint32_t cnt[8],
+                                                  const uint32_t roff[8], uint32_t prim_base) {
+#pragma unroll
+    for (int g = 0; g < 8; g += G) {
+        uint4 buf[G][RW];
+#pragma unroll
+        for (int s = 0; s < G; ++s)
+            if ((leafc >> (g + s)) & 1u)
+#pragma unroll
+                for (int w = 0; w < RW; ++w) buf[s][w] = __ldg(a.recs_in + (size_t)id0[g + s] * RW + w);
+#pragma unroll
+        for (int s = 0; s < G; ++s)
+            if ((leafc >> (g + s)) & 1u)
+#pragma unroll
+                for (int w = 0; w < RW; ++w) a.recs_out[(size_t)(prim_base + roff[g + s]) * RW + w] = buf[s][w];
+    }
+    for (int s = 0; s < 8; ++s) {
+        if (!((leafc >> s) & 1u)) continue;
+        for (uint32_t j = 1; j < cnt[s]; ++j) {
+            const uint4 *sr = a.recs_in + (size_t)__ldg(a.ids + first[s] + j) * RW;
+            uint4 *dr = a.recs_out + (size_t)(prim_base + roff[s] + j) * RW;
+#pragma unroll
+            for (int w = 0; w < RW; ++w) dr[w] = __ldg(sr + w);
+        }
+    }
+}
+
+// Phase B: writes wide node k with its child and record bases.  The node's
+// reference and slots, then every slot's box, SAH flag and binary node, then
+// the record ids are each one round of independent loads.
 __device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t child_base, uint32_t prim_base) {
     const uint32_t src = __ldcg(a.wq + k);
+    const uint4 *sp = reinterpret_cast<const uint4 *>(a.slots + (size_t)k * 8u);
+    const uint4 s0 = __ldcg(sp), s1 = __ldcg(sp + 1);
+    const uint32_t slot_ref[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
     const Box node = ref_box(a, src);
-    uint32_t slot_ref[8];
     Box sbox[8];
     bool used[8];
-    for (int s = 0; s < 8; ++s) {
-        slot_ref[s] = __ldcg(a.slots + (size_t)k * 8u + s);
-        used[s] = slot_ref[s] != kNone;
-        if (used[s]) sbox[s] = ref_box(a, slot_ref[s]);
-        else sbox[s] = box_empty();
-    }
-    uint8_t meta[8];
-    uint32_t imask = 0, off = 0, ichild = 0;
+    uint32_t first[8], cnt[8], openm = 0u;
+#pragma unroll
     for (int s = 0; s < 8; ++s) {
         const uint32_t r = slot_ref[s];
+        used[s] = r != kNone;
+        sbox[s] = box_empty();
+        first[s] = 0u;
+        cnt[s] = 0u;
+        if (!used[s]) continue;
+        const bool leaf = ref_is_leaf(r);
+        const uint32_t i = r & ~kLeafBit;
+        sbox[s] = ref_box(a, r);
+        uint4 nd = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t lf = 1u;
+        if (!leaf) {
+            nd = __ldg(a.bin + i);
+            lf = __ldg(a.leafable + i);
+        }
+        if (!leaf && lf == 0u) openm |= 1u << s;
+        first[s] = leaf ? i : nd.z;
+        cnt[s] = leaf ? 1u : nd.w - nd.z + 1u;
+    }
+    uint8_t meta[8];
+    uint32_t roff[8], id0[8], leafc = 0u, off = 0u, ichild = 0u;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
         meta[s] = 0;
-        if (r == kNone) continue;
-        if (ref_openable(a, r)) {
-            imask |= 1u << s;
+        roff[s] = 0u;
+        id0[s] = 0u;
+        if (!used[s]) continue;
+        if ((openm >> s) & 1u) {
             meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
-            uint32_t dst = child_base + ichild++;
-            if (dst < a.capacity) a.wq[dst] = r;
+            const uint32_t dst = child_base + ichild++;
+            if (dst < a.capacity) a.wq[dst] = slot_ref[s];
             else report_error(a.err, RT_ERR_BOUNDS, 0x60000000u | k);
         } else {
-            uint32_t first, last;
-            if (ref_is_leaf(r)) { first = last = r & ~kLeafBit; }
-            else { uint4 nd = a.bin[r]; first = nd.z; last = nd.w; }
-            uint32_t cnt = last - first + 1u;
-            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | off);
-            for (uint32_t j = 0; j < cnt; ++j) {
-                const uint4 *srcr = a.recs_in + (size_t)a.ids[first + j] * a.rec_words;
-                uint4 *dstr = a.recs_out + (size_t)(prim_base + off + j) * a.rec_words;
-                for (uint32_t w = 0; w < a.rec_words; ++w) dstr[w] = srcr[w];
-            }
-            off += cnt;
+            meta[s] = (uint8_t)((((1u << cnt[s]) - 1u) << 5) | off);
+            roff[s] = off;
+            leafc |= 1u << s;
+            id0[s] = __ldg(a.ids + first[s]);
+            off += cnt[s];
         }
     }
     uint4 *o = a.nodes_out + (size_t)k * 5u;
-    encode_node(node, sbox, used, imask, o);
+    encode_node(node, sbox, used, openm, o);
     o[1] = make_uint4(child_base, prim_base, pack_meta4(meta), pack_meta4(meta + 4));
+    if (a.rec_words == 3u) copy_leaf_records<3, 4>(a, leafc, id0, first, cnt, roff, prim_base);
+    else copy_leaf_records<5, 2>(a, leafc, id0, first, cnt, roff, prim_base);
 }
 
 template <int N>

@@ -40,7 +40,7 @@ enum {
     RT_ERR_CUDA = -3,        /* a CUDA runtime call failed                   */
     RT_ERR_TIMEOUT = -4,     /* a bounded device-side wait ran out           */
     RT_ERR_BOUNDS = -5,      /* a device-side bounds check fired             */
-    RT_ERR_UNSUPPORTED = -6, /* valid request this build does not implement  */
+    RT_ERR_UNSUPPORTED = -6, /* valid request the library does not implement */
     RT_ERR_NO_DEVICE = -7,   /* no CUDA device / kernel image for it         */
     RT_ERR_NOT_FOUND = -8    /* a lookup (tuning cache) found no entry       */
 };
