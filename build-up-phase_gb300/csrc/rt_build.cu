@@ -13,10 +13,11 @@
 //   karras    binary radix tree over the sorted keys (Karras, HPG 2012),
 //             index-augmented keys for duplicates
 //   refit     bottom-up boxes + SAH leaf decisions (one atomic per node)
-//   collapse  one cooperative kernel, breadth-first level by level: greedy
-//             widening to 8 children, octant slot assignment, 8-bit child-box
-//             quantisation (Ylitie, Karras, Laine, HPG 2017), leaf records
-//             gathered into node order.  Node and record positions come from
+//   collapse  one cooperative kernel, breadth-first level by level, eight
+//             lanes per wide node: greedy widening to 8 children, octant slot
+//             assignment, 8-bit child-box quantisation (Ylitie, Karras,
+//             Laine, HPG 2017); then every leaf record gathered into node
+//             order by one thread each.  Node and record positions come from
 //             grid-wide prefix sums, so the output is deterministic and equal
 //             byte for byte to the CPU restatement of the same steps.
 #include <cooperative_groups.h>
@@ -45,7 +46,7 @@ struct GeomParams {
 
 struct BuildLayout {
     uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, parent, node_box, node_cost, leafable, visit, leaf_box,
-        wq, slots, counts, blk, misc, sort, total;
+        wq, slots, desc, counts, blk, misc, sort, total;
 };
 
 inline uint32_t node_capacity_for(uint32_t n) { return n < 2 ? 1u : n - 1u; }
@@ -82,6 +83,7 @@ BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
     L.leaf_box = take((uint64_t)n * 32u);
     L.wq = take(cap * 4u);
     L.slots = take(cap * 32u);
+    L.desc = take(cap * 4u);
     L.counts = take(cap * 4u);
     L.blk = take((uint64_t)kMaxCoopBlocks * 8u);
     L.misc = take(256);
@@ -438,13 +440,31 @@ struct RefitArgs {
     uint32_t *err;
 };
 
+// Arrival at a binary node: increments its counter with release (this
+// thread's earlier stores -- its subtree's box and cost -- are visible to the
+// thread that reads the new value) and acquire (the first arrival's stores
+// are visible to this thread's later loads) at device scope.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+// One thread per leaf climbs towards the root; the second thread to arrive
+// at a node computes it.  The climbing thread keeps its own subtree's box and
+// cost in registers and loads only the sibling's; the node's children and
+// parent (read-only here) are loaded before the arrival so their latency
+// overlaps the atomic.
 __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.n) return;
-    Box lb = load_box(a.boxes, a.ids[j]);
+    const Box lb = load_box(a.boxes, a.ids[j]);
     store_box(a.leaf_box, j, lb);
     if (a.n < 2) return;
-    uint32_t p = a.parent[a.n - 1 + j];
+    uint32_t me = kLeafBit | j;
+    Box mb = lb;
+    float mcost = RT_SAH_PRIM;
+    uint32_t p = __ldg(a.parent + a.n - 1 + j);
     // A radix tree over 2^30 keys is at most 96 levels deep (63 key bits +
     // 32 index bits); the cap only guards against a corrupt parent chain.
     for (int climb = 0; p != kNone; ++climb) {
@@ -452,31 +472,35 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
             report_error(a.err, RT_ERR_BOUNDS, 0x61000000u | j);
             return;
         }
-        __threadfence();
-        if (atomicAdd(&a.visit[p], 1u) == 0u) return;
-        __threadfence();
-        uint4 nd = a.bin[p];
-        const bool ll = nd.x & kLeafBit, rl = nd.y & kLeafBit;
-        Box bl = ll ? load_box(a.leaf_box, nd.x & ~kLeafBit) : load_box(a.node_box, nd.x);
-        Box br = rl ? load_box(a.leaf_box, nd.y & ~kLeafBit) : load_box(a.node_box, nd.y);
-        float cl = ll ? RT_SAH_PRIM : __ldcg(a.node_cost + nd.x);
-        float cr = rl ? RT_SAH_PRIM : __ldcg(a.node_cost + nd.y);
-        Box b = box_union(bl, br);
-        float an = half_area(b);
+        const uint4 nd = __ldg(a.bin + p);
+        const uint32_t pp = __ldg(a.parent + p);
+        if (arrive_acq_rel(a.visit + p) == 0u) return;
+        const bool left = nd.x == me;
+        const uint32_t sib = left ? nd.y : nd.x;
+        const bool sl = (sib & kLeafBit) != 0u;
+        const Box sb = sl ? load_box(a.leaf_box, sib & ~kLeafBit) : load_box(a.node_box, sib);
+        const float scost = sl ? RT_SAH_PRIM : __ldcg(a.node_cost + sib);
+        const Box &bl = left ? mb : sb, &br = left ? sb : mb;
+        const float cl = left ? mcost : scost, cr = left ? scost : mcost;
+        const Box b = box_union(bl, br);
+        const float an = half_area(b);
         float split;
         if (an > 0.0f) {
-            float s = half_area(bl) * cl + half_area(br) * cr;
-            split = RT_SAH_NODE + s / an;
+            const float sah = half_area(bl) * cl + half_area(br) * cr;
+            split = RT_SAH_NODE + sah / an;
         } else {
             split = RT_SAH_NODE + (cl + cr);
         }
-        uint32_t count = nd.w - nd.z + 1u;
-        float leaf = (float)count * RT_SAH_PRIM;
-        bool lf = count <= (uint32_t)RT_MAX_LEAF_PRIMS && leaf <= split;
+        const uint32_t count = nd.w - nd.z + 1u;
+        const float leaf = (float)count * RT_SAH_PRIM;
+        const bool lf = count <= (uint32_t)RT_MAX_LEAF_PRIMS && leaf <= split;
+        mcost = lf ? leaf : split;
         store_box(a.node_box, p, b);
-        a.node_cost[p] = lf ? leaf : split;
+        a.node_cost[p] = mcost;
         a.leafable[p] = lf ? 1 : 0;
-        p = a.parent[p];
+        mb = b;
+        me = p;
+        p = pp;
     }
 }
 
@@ -487,18 +511,16 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
 struct CollapseArgs {
     uint32_t n;
     uint32_t width;      // children per wide node, 4..8
-    uint32_t rec_words;  // uint4 words per leaf record (3 or 5)
     uint32_t capacity;
     uint32_t root_ref;
-    const uint4 *recs_in;
-    uint4 *recs_out;
-    const uint32_t *ids;
+    uint32_t *gather;  // per leaf record in node order: its sorted primitive
     const uint4 *bin;
     const float *node_box;
     const uint8_t *leafable;
     const float *leaf_box;
     uint32_t *wq;
     uint32_t *slots;
+    uint32_t *desc;
     uint32_t *counts;
     uint32_t *blk;
     uint4 *nodes_out;
@@ -518,7 +540,7 @@ __device__ __forceinline__ Box ref_box(const CollapseArgs &a, uint32_t r) {
 // child and step.
 struct RefInfo {
     uint32_t ref;
-    uint32_t kid0, kid1;  // binary children (internal references)
+    uint32_t kid0, kid1;  // binary children of an opened node; kid0 of a leaf child: its first sorted primitive
     uint32_t cnt;         // primitives below; bit 31: internal and not a SAH leaf (gets widened)
     float area;           // half surface area of the box
 };
@@ -546,254 +568,314 @@ __device__ __forceinline__ RefInfo fetch_ref(const CollapseArgs &a, uint32_t r) 
     }
     RefInfo x;
     x.ref = r;
-    x.kid0 = nd.x;
+    const bool open = !leaf && lf == 0u;
+    x.kid0 = leaf ? i : (open ? nd.x : nd.z);
     x.kid1 = nd.y;
-    x.cnt = (leaf ? 1u : nd.w - nd.z + 1u) | ((!leaf && lf == 0u) ? kOpenBit : 0u);
+    x.cnt = (leaf ? 1u : nd.w - nd.z + 1u) | (open ? kOpenBit : 0u);
     x.area = half_area(b);
     return x;
 }
 __device__ __forceinline__ bool info_open(const RefInfo &x) { return (x.cnt & kOpenBit) != 0u; }
 
-// Greedy widening: while fewer than `width` children, open the openable
-// child of largest surface area (the first on ties).  Arrays are indexed by
-// unrolled compare-and-select so they stay in registers.
-__device__ __forceinline__ int collapse_children(const CollapseArgs &a, const RefInfo &src, RefInfo ch[8]) {
-    if (!info_open(src)) {
-        ch[0] = src;
-        return 1;
-    }
-    ch[0] = fetch_ref(a, src.kid0);
-    ch[1] = fetch_ref(a, src.kid1);
-    int n = 2;
-    while (n < (int)a.width) {
-        int best = -1;
-        float best_a = -1.0f;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if (i < n && info_open(ch[i]) && ch[i].area > best_a) { best_a = ch[i].area; best = i; }
-        if (best < 0) break;
-        uint32_t k0 = 0u, k1 = 0u;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if (i == best) { k0 = ch[i].kid0; k1 = ch[i].kid1; }
-        const RefInfo x0 = fetch_ref(a, k0), x1 = fetch_ref(a, k1);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (i == best) ch[i] = x0;
-            if (i == n) ch[i] = x1;
-        }
-        ++n;
-    }
-    return n;
-}
-
-// Octant slot of each child: repeatedly the (child, slot) pair of least
-// cost (x + y) + z, the centre offset signed by the slot's octant, the first
-// pair in (child, slot) order on ties.  The child boxes are reloaded here (L1
-// hits: the widening has just fetched them).  Returns the slot of child c in
-// bits 4c..4c+3.
-__device__ __forceinline__ uint32_t assign_slots(const CollapseArgs &a, uint32_t src, const RefInfo ch[8], int n) {
-    const Box node = load_box_ro(a, src);
-    const bool ne = box_is_empty(node);
-    float ncen[3], diff[8][3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) ncen[q] = (node.lo[q] + node.hi[q]) * 0.5f;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        Box cb = box_empty();
-        if (c < n) cb = load_box_ro(a, ch[c].ref);
-        const bool ce = box_is_empty(cb);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) diff[c][q] = (ce || ne) ? 0.0f : (cb.lo[q] + cb.hi[q]) * 0.5f - ncen[q];
-    }
-    uint32_t used = 0u, done = 0u, code = 0u;
-    for (int it = 0; it < n; ++it) {
-        int bc = -1, bs = -1;
-        float bv = kInf;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            if (c >= n || ((done >> c) & 1u)) continue;
-#pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                if ((used >> s) & 1u) continue;
-                const float x = (s & 1) ? -diff[c][0] : diff[c][0];
-                const float y = (s & 2) ? -diff[c][1] : diff[c][1];
-                const float z = (s & 4) ? -diff[c][2] : diff[c][2];
-                const float cost = (x + y) + z;
-                if (bc < 0 || cost < bv) { bc = c; bs = s; bv = cost; }
-            }
-        }
-        done |= 1u << bc;
-        used |= 1u << bs;
-        code |= (uint32_t)bs << (4 * bc);
-    }
-    return code;
-}
-
-// Phase A: children and slots of wide node k; returns (n_int, n_prim).
-__device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, uint32_t &n_int, uint32_t &n_prim) {
-    // wq, slots and counts are written by other blocks of this launch between
-    // grid barriers: read them through L2 (__ldcg), never a stale L1 line.
-    const uint32_t sref = __ldcg(a.wq + k);
-    RefInfo ch[8];
-    const int nc = collapse_children(a, fetch_ref(a, sref), ch);
-    const uint32_t code = assign_slots(a, sref, ch, nc);
-    uint32_t slot_ref[8] = {kNone, kNone, kNone, kNone, kNone, kNone, kNone, kNone};
-    uint32_t ni = 0, np = 0;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        if (c >= nc) continue;
-        const uint32_t s = (code >> (4 * c)) & 0xfu;
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
-            if ((uint32_t)t == s) slot_ref[t] = ch[c].ref;
-        if (info_open(ch[c])) ++ni;
-        else np += ch[c].cnt;
-    }
-    uint4 *o = reinterpret_cast<uint4 *>(a.slots + (size_t)k * 8u);
-    o[0] = make_uint4(slot_ref[0], slot_ref[1], slot_ref[2], slot_ref[3]);
-    o[1] = make_uint4(slot_ref[4], slot_ref[5], slot_ref[6], slot_ref[7]);
-    n_int = ni;
-    n_prim = np;
-}
-
-// Origin, per-axis power-of-two scales and the 8-bit child boxes of a wide
-// node (words 0, 2, 3, 4 of its five; word 1 holds the child and record
-// bases and the slot metadata): the boxes are rounded outward (lower bounds
-// down, upper bounds up) so the quantised box contains the exact one.  Shared
-// by the build and the refit.
-__device__ void encode_node(const Box &node, const Box sbox[8], const bool used[8], uint32_t imask, uint4 *o) {
-    const bool empty = box_is_empty(node);
+// Quantisation frame of a wide node: the origin (lower corner) and per-axis
+// power-of-two scales of its 8-bit child boxes.
+struct QFrame {
     float p[3];
     int e[3];
+    bool empty;
+};
+
+__device__ __forceinline__ QFrame node_frame(const Box &node) {
+    QFrame f;
+    f.empty = box_is_empty(node);
+#pragma unroll
     for (int q = 0; q < 3; ++q) {
-        p[q] = empty ? 0.0f : node.lo[q];
-        e[q] = empty ? 0 : qexp_for(__fsub_ru(node.hi[q], p[q]));
+        f.p[q] = f.empty ? 0.0f : node.lo[q];
+        f.e[q] = f.empty ? 0 : qexp_for(__fsub_ru(node.hi[q], f.p[q]));
     }
-    uint8_t qlo[3][8], qhi[3][8];
+    return f;
+}
+
+// 8-bit bounds of a child box in the frame, rounded outward (lower bounds
+// down, upper bounds up) so the quantised box contains the exact one; an
+// unused slot, an empty node or an empty child gets the inverted box
+// (255, 0).
+__device__ __forceinline__ void quantise_child(const QFrame &f, bool used, const Box &b, uint32_t ql[3],
+                                               uint32_t qh[3]) {
+    const bool inv = !used || f.empty || box_is_empty(b);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ql[a] = 255u;
+        qh[a] = 0u;
+        if (inv) continue;
+        const float sc = pow2f(-f.e[a]);
+        const float dl = __fsub_rd(b.lo[a], f.p[a]) * sc;
+        const float dh_raw = __fsub_ru(b.hi[a], f.p[a]);
+        const float dh = dh_raw * sc;
+        const float fl = floorf(dl), fh = ceilf(dh);
+        ql[a] = fl < 0.0f ? 0u : (fl > 255.0f ? 255u : (uint32_t)(int)fl);
+        qh[a] = fh < 0.0f ? 0u : (fh > 255.0f ? 255u : (uint32_t)(int)fh);
+        if (qh[a] == 0u && dh_raw > 0.0f) qh[a] = 1u;
+    }
+}
+
+// Word 0 of a wide node: origin, exponents and internal-child mask.
+__device__ __forceinline__ uint4 frame_word(const QFrame &f, uint32_t imask) {
+    const uint32_t w = ((uint32_t)(uint8_t)(int8_t)f.e[0]) | ((uint32_t)(uint8_t)(int8_t)f.e[1] << 8) |
+                       ((uint32_t)(uint8_t)(int8_t)f.e[2] << 16) | (imask << 24);
+    return make_uint4(__float_as_uint(f.p[0]), __float_as_uint(f.p[1]), __float_as_uint(f.p[2]), w);
+}
+
+// Words 0, 2, 3, 4 of a wide node from its box and its slots' boxes: the
+// child boxes as six byte planes (lo x, lo y, lo z, hi x, hi y, hi z), byte s
+// of a plane for slot s.  Used by the refit; the build's phase A writes the
+// same bytes one slot per lane.
+__device__ void encode_node(const Box &node, const Box sbox[8], const bool used[8], uint32_t imask, uint4 *o) {
+    const QFrame f = node_frame(node);
+    uint32_t q[12] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
     for (int s = 0; s < 8; ++s) {
-        const bool inv = !used[s] || empty || box_is_empty(sbox[s]);
+        uint32_t ql[3], qh[3];
+        quantise_child(f, used[s], sbox[s], ql, qh);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            q[2 * a + (s >> 2)] |= ql[a] << (8 * (s & 3));
+            q[6 + 2 * a + (s >> 2)] |= qh[a] << (8 * (s & 3));
+        }
+    }
+    o[0] = frame_word(f, imask);
+    o[2] = make_uint4(q[0], q[1], q[2], q[3]);
+    o[3] = make_uint4(q[4], q[5], q[6], q[7]);
+    o[4] = make_uint4(q[8], q[9], q[10], q[11]);
+}
+
+// ---------------------------------------------------------------------------
+// Phase A, eight lanes per wide node.  Lane j of an aligned group of eight
+// holds child j during the widening and the slot assignment, and the group's
+// choices are made with shuffles (every lane reaches the same result), so a
+// node costs one round trip per widening step and a few hundred instructions
+// per lane.  Every loop that shuffles is warp-uniform: all 32 lanes run each
+// shuffle, groups that are done (or hold no node) take part with `act` off.
+// ---------------------------------------------------------------------------
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Lane (0-7) of the largest key among the group's lanes with `ok`, the
+// lowest lane on ties; -1 if none.  Keys are > -1 (never NaN) where `ok`.
+__device__ __forceinline__ int group_argmax(float key, bool ok) {
+    float v = ok ? key : -1.0f;
+    int i = ok ? (int)(threadIdx.x & 7u) : 8;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const float v2 = __shfl_xor_sync(kFullMask, v, o);
+        const int i2 = __shfl_xor_sync(kFullMask, i, o);
+        if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+    }
+    return i < 8 ? i : -1;
+}
+
+// Lane of the least key among the lanes with `ok`, the lowest lane on ties;
+// -1 if none.  Keys are never NaN where `ok`.
+__device__ __forceinline__ int group_argmin(float key, bool ok) {
+    float v = ok ? key : kInf;
+    int i = ok ? (int)(threadIdx.x & 7u) : 8;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const float v2 = __shfl_xor_sync(kFullMask, v, o);
+        const int i2 = __shfl_xor_sync(kFullMask, i, o);
+        if (v2 < v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+    }
+    return i < 8 ? i : -1;
+}
+
+// Phase A of wide node k (the lanes of a group with `valid` false take part
+// in the shuffles only):
+//  - widening: while fewer than `width` children, open the openable child of
+//    largest surface area, the first on ties;
+//  - slots: repeatedly the (child, slot) pair of least cost (x + y) + z, the
+//    centre offset signed by the slot's octant.  The sequential scan in
+//    (child, slot) order keeps its first pair when that pair's cost is NaN
+//    (nothing compares below NaN) and otherwise ends on the first least
+//    non-NaN pair; each lane finds its own child's first least non-NaN slot
+//    and the group takes the least of those, or the first pair when its
+//    cost is NaN -- the same choice;
+//  - words 0, 2, 3, 4 of the node, the child boxes stored as bytes, one
+//    slot per lane.
+// Leaves for phase B, per slot, the child node (internal) or the first
+// sorted primitive (leaf) in `slots`, and in `desc` the internal-child mask
+// (bits 0-7) and each leaf slot's primitive count minus one (two bits per
+// slot from bit 8).  Returns the node's internal children and primitives
+// (every lane of the group).
+__device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, uint32_t &n_int, uint32_t &n_prim) {
+    const int j = (int)(threadIdx.x & 7u);
+    const int gb = (int)(threadIdx.x & 24u);
+    // wq and the hand-off arrays are written by other blocks of this launch
+    // between grid barriers: read through L2 (__ldcg), never a stale L1 line.
+    uint32_t sref = 0u;
+    RefInfo src = {0u, 0u, 0u, 0u, 0.0f};
+    if (valid) {
+        sref = __ldcg(a.wq + k);
+        src = fetch_ref(a, sref);
+    }
+    RefInfo mine = {0u, 0u, 0u, 0u, 0.0f};
+    int n = 0;
+    if (valid) {
+        if (!info_open(src)) {
+            n = 1;
+            if (j == 0) mine = src;
+        } else {
+            n = 2;
+            if (j < 2) mine = fetch_ref(a, j == 0 ? src.kid0 : src.kid1);
+        }
+    }
+    bool act = valid && info_open(src);
+    for (;;) {
+        act = act && n < (int)a.width;
+        if (!__any_sync(kFullMask, act)) break;
+        const int best = group_argmax(mine.area, act && j < n && info_open(mine) && mine.area > -1.0f);
+        const int from = gb | (best < 0 ? 0 : best);
+        const uint32_t k0 = __shfl_sync(kFullMask, mine.kid0, from);
+        const uint32_t k1 = __shfl_sync(kFullMask, mine.kid1, from);
+        if (best < 0) act = false;
+        if (act) {
+            if (j == best) mine = fetch_ref(a, k0);
+            else if (j == n) mine = fetch_ref(a, k1);
+            ++n;
+        }
+    }
+
+    // slot costs of this lane's child
+    const Box nb = valid ? load_box_ro(a, sref) : box_empty();
+    const bool have = valid && j < n;
+    const Box cb = have ? load_box_ro(a, mine.ref) : box_empty();
+    const bool ne = box_is_empty(nb), ce = box_is_empty(cb);
+    float d[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float ncen = (nb.lo[q] + nb.hi[q]) * 0.5f;
+        d[q] = (ce || ne) ? 0.0f : (cb.lo[q] + cb.hi[q]) * 0.5f - ncen;
+    }
+    float cost[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const float x = (s & 1) ? -d[0] : d[0];
+        const float y = (s & 2) ? -d[1] : d[1];
+        const float z = (s & 4) ? -d[2] : d[2];
+        cost[s] = (x + y) + z;
+    }
+    uint32_t used = 0u;
+    int my_slot = -1;
+    for (int it = 0; it < 8; ++it) {
+        const bool go = valid && it < n;
+        if (!__any_sync(kFullMask, go)) break;
+        const bool cand = go && j < n && my_slot < 0;
+        const int s0 = __ffs((int)(~used & 0xffu)) - 1;
+        float c0 = 0.0f, v = kInf;
+        int vs = -1;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (s == s0) c0 = cost[s];
+            if (((used >> s) & 1u) == 0u && !isnan(cost[s]) && (vs < 0 || cost[s] < v)) {
+                v = cost[s];
+                vs = s;
+            }
+        }
+        const uint32_t cm = (__ballot_sync(kFullMask, cand) >> gb) & 0xffu;
+        const int l0 = __ffs((int)cm) - 1;
+        const bool nan0 = __shfl_sync(kFullMask, isnan(c0) ? 1 : 0, gb | (l0 < 0 ? 0 : l0)) != 0;
+        int bc = group_argmin(v, cand && vs >= 0);
+        int bs = __shfl_sync(kFullMask, vs, gb | (bc < 0 ? 0 : bc));
+        if (nan0) {
+            bc = l0;
+            bs = s0;
+        }
+        if (go && bc >= 0) {
+            if (j == bc) my_slot = bs;
+            used |= 1u << bs;
+        }
+    }
+
+    // phase-B hand-off and the node's counts
+    const bool open = have && info_open(mine);
+    const uint32_t cnt = mine.cnt & ~kOpenBit;
+    uint32_t dbits = 0u, tally = 0u;
+    if (have && my_slot >= 0) {
+        if (open) {
+            dbits = 1u << my_slot;
+            tally = 1u;
+        } else {
+            dbits = (cnt - 1u) << (8 + 2 * my_slot);
+            tally = cnt << 16;
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        dbits |= __shfl_xor_sync(kFullMask, dbits, o);
+        tally += __shfl_xor_sync(kFullMask, tally, o);
+    }
+    n_int = tally & 0xffffu;
+    n_prim = tally >> 16;
+    if (!valid) return;
+
+    const QFrame f = node_frame(nb);
+    uint8_t *nbytes = reinterpret_cast<uint8_t *>(a.nodes_out + (size_t)k * 5u);
+    if (have && my_slot >= 0) {
+        uint32_t ql[3], qh[3];
+        quantise_child(f, true, cb, ql, qh);
+#pragma unroll
         for (int q = 0; q < 3; ++q) {
-            if (inv) { qlo[q][s] = 255; qhi[q][s] = 0; continue; }
-            float sc = pow2f(-e[q]);
-            float dl = __fsub_rd(sbox[s].lo[q], p[q]) * sc;
-            float dh_raw = __fsub_ru(sbox[s].hi[q], p[q]);
-            float dh = dh_raw * sc;
-            float fl = floorf(dl), fh = ceilf(dh);
-            int ql = fl < 0.0f ? 0 : (fl > 255.0f ? 255 : (int)fl);
-            int qh = fh < 0.0f ? 0 : (fh > 255.0f ? 255 : (int)fh);
-            if (qh == 0 && dh_raw > 0.0f) qh = 1;
-            qlo[q][s] = (uint8_t)ql;
-            qhi[q][s] = (uint8_t)qh;
+            nbytes[32 + 8 * q + my_slot] = (uint8_t)ql[q];
+            nbytes[56 + 8 * q + my_slot] = (uint8_t)qh[q];
         }
+        a.slots[(size_t)k * 8u + my_slot] = open ? mine.ref : mine.kid0;
     }
-    auto pack4 = [](const uint8_t *b) {
-        return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
-    };
-    uint32_t w0w = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
-                   ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
-    o[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), w0w);
-    o[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
-    o[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
-    o[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
-}
-
-__device__ __forceinline__ uint32_t pack_meta4(const uint8_t *b) {
-    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
-}
-
-// Leaf records of one wide node, gathered from input order into node order.
-// The first record of each leaf child is loaded G children at a time before
-// any is stored, so the loads overlap; the further primitives of collapsed
-// subtrees (at most RT_MAX_LEAF_PRIMS - 1 per child) follow.
-template <int RW, int G>
-__device__ __forceinline__ void copy_leaf_records(const CollapseArgs &a, const uint32_t leafc, const uint32_t id0[8],
-                                                  const uint32_t first[8], const uint32_t cnt[8],
-                                                  const uint32_t roff[8], uint32_t prim_base) {
+    if (((used >> j) & 1u) == 0u) {
 #pragma unroll
-    for (int g = 0; g < 8; g += G) {
-        uint4 buf[G][RW];
-#pragma unroll
-        for (int s = 0; s < G; ++s)
-            if ((leafc >> (g + s)) & 1u)
-#pragma unroll
-                for (int w = 0; w < RW; ++w) buf[s][w] = __ldg(a.recs_in + (size_t)id0[g + s] * RW + w);
-#pragma unroll
-        for (int s = 0; s < G; ++s)
-            if ((leafc >> (g + s)) & 1u)
-#pragma unroll
-                for (int w = 0; w < RW; ++w) a.recs_out[(size_t)(prim_base + roff[g + s]) * RW + w] = buf[s][w];
-    }
-    for (int s = 0; s < 8; ++s) {
-        if (!((leafc >> s) & 1u)) continue;
-        for (uint32_t j = 1; j < cnt[s]; ++j) {
-            const uint4 *sr = a.recs_in + (size_t)__ldg(a.ids + first[s] + j) * RW;
-            uint4 *dr = a.recs_out + (size_t)(prim_base + roff[s] + j) * RW;
-#pragma unroll
-            for (int w = 0; w < RW; ++w) dr[w] = __ldg(sr + w);
+        for (int q = 0; q < 3; ++q) {
+            nbytes[32 + 8 * q + j] = 255;
+            nbytes[56 + 8 * q + j] = 0;
         }
+        a.slots[(size_t)k * 8u + j] = kNone;
+    }
+    if (j == 0) {
+        a.nodes_out[(size_t)k * 5u] = frame_word(f, dbits & 0xffu);
+        a.desc[k] = dbits;
     }
 }
 
-// Phase B: writes wide node k with its child and record bases.  The node's
-// reference and slots, then every slot's box, SAH flag and binary node, then
-// the record ids are each one round of independent loads.
+// Phase B of wide node k, once its child and record bases are known: word 1
+// of the node (bases and slot metadata), its internal children appended to
+// the next level's queue, and for each of its leaf records the sorted
+// primitive it holds (the gather map; k_gather_records moves the records).
 __device__ void collapse_phase_b(const CollapseArgs &a, uint32_t k, uint32_t child_base, uint32_t prim_base) {
-    const uint32_t src = __ldcg(a.wq + k);
     const uint4 *sp = reinterpret_cast<const uint4 *>(a.slots + (size_t)k * 8u);
     const uint4 s0 = __ldcg(sp), s1 = __ldcg(sp + 1);
-    const uint32_t slot_ref[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-    const Box node = ref_box(a, src);
-    Box sbox[8];
-    bool used[8];
-    uint32_t first[8], cnt[8], openm = 0u;
+    const uint32_t desc = __ldcg(a.desc + k);
+    const uint32_t slot[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+    uint32_t meta_lo = 0u, meta_hi = 0u, off = 0u, ichild = 0u;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
-        const uint32_t r = slot_ref[s];
-        used[s] = r != kNone;
-        sbox[s] = box_empty();
-        first[s] = 0u;
-        cnt[s] = 0u;
-        if (!used[s]) continue;
-        const bool leaf = ref_is_leaf(r);
-        const uint32_t i = r & ~kLeafBit;
-        sbox[s] = ref_box(a, r);
-        uint4 nd = make_uint4(0u, 0u, 0u, 0u);
-        uint32_t lf = 1u;
-        if (!leaf) {
-            nd = __ldg(a.bin + i);
-            lf = __ldg(a.leafable + i);
-        }
-        if (!leaf && lf == 0u) openm |= 1u << s;
-        first[s] = leaf ? i : nd.z;
-        cnt[s] = leaf ? 1u : nd.w - nd.z + 1u;
-    }
-    uint8_t meta[8];
-    uint32_t roff[8], id0[8], leafc = 0u, off = 0u, ichild = 0u;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        meta[s] = 0;
-        roff[s] = 0u;
-        id0[s] = 0u;
-        if (!used[s]) continue;
-        if ((openm >> s) & 1u) {
-            meta[s] = (uint8_t)((1u << 5) | (24u + (uint32_t)s));
+        if (slot[s] == kNone) continue;
+        uint32_t m;
+        if ((desc >> s) & 1u) {
+            m = (1u << 5) | (24u + (uint32_t)s);
             const uint32_t dst = child_base + ichild++;
-            if (dst < a.capacity) a.wq[dst] = slot_ref[s];
+            if (dst < a.capacity) a.wq[dst] = slot[s];
             else report_error(a.err, RT_ERR_BOUNDS, 0x60000000u | k);
         } else {
-            meta[s] = (uint8_t)((((1u << cnt[s]) - 1u) << 5) | off);
-            roff[s] = off;
-            leafc |= 1u << s;
-            id0[s] = __ldg(a.ids + first[s]);
-            off += cnt[s];
+            const uint32_t c = ((desc >> (8u + 2u * s)) & 3u) + 1u;
+            m = (((1u << c) - 1u) << 5) | off;
+            for (uint32_t j = 0; j < c; ++j) {
+                const uint32_t d = prim_base + off + j;
+                if (d < a.n) a.gather[d] = slot[s] + j;
+                else report_error(a.err, RT_ERR_BOUNDS, 0x63000000u | k);
+            }
+            off += c;
         }
+        if (s < 4) meta_lo |= m << (8 * s);
+        else meta_hi |= m << (8 * (s - 4));
     }
-    uint4 *o = a.nodes_out + (size_t)k * 5u;
-    encode_node(node, sbox, used, openm, o);
-    o[1] = make_uint4(child_base, prim_base, pack_meta4(meta), pack_meta4(meta + 4));
-    if (a.rec_words == 3u) copy_leaf_records<3, 4>(a, leafc, id0, first, cnt, roff, prim_base);
-    else copy_leaf_records<5, 2>(a, leafc, id0, first, cnt, roff, prim_base);
+    a.nodes_out[(size_t)k * 5u + 1u] = make_uint4(child_base, prim_base, meta_lo, meta_hi);
 }
 
 template <int N>
@@ -849,12 +931,17 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
         const uint32_t chunk = (level_count + G - 1u) / G;
         const uint32_t c0 = min(b * chunk, level_count), c1 = min(c0 + chunk, level_count);
         uint32_t my_int = 0, my_prim = 0;
-        for (uint32_t k = c0 + t; k < c1; k += kCollapseThreads) {
+        // eight lanes per node (collapse_phase_a); the loop is block-uniform
+        for (uint32_t kb = c0; kb < c1; kb += kCollapseThreads / 8u) {
+            const uint32_t k = kb + (t >> 3);
+            const bool valid = k < c1;
             uint32_t ni, np;
-            collapse_phase_a(a, level_start + k, ni, np);
-            a.counts[level_start + k] = ni | (np << 16);
-            my_int += ni;
-            my_prim += np;
+            collapse_phase_a(a, level_start + k, valid, ni, np);
+            if (valid && (t & 7u) == 0u) {
+                a.counts[level_start + k] = ni | (np << 16);
+                my_int += ni;
+                my_prim += np;
+            }
         }
         my_int = block_sum<kCollapseThreads>(my_int, s_red);
         my_prim = block_sum<kCollapseThreads>(my_prim, s_red);
@@ -898,6 +985,24 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
         a.hdr->bounds_lo[3] = 0.0f;
         a.hdr->bounds_hi[3] = 0.0f;
     }
+}
+
+// Leaf records in node order: record d is the input record of sorted
+// primitive gather[d] (written by the collapse's phase B).  One thread per
+// record; the grid covers every record.
+template <int RW>
+__global__ void __launch_bounds__(256) k_gather_records(const uint4 *__restrict__ recs_in, uint4 *__restrict__ recs_out,
+                                                        const uint32_t *__restrict__ ids,
+                                                        const uint32_t *__restrict__ gather, uint32_t n) {
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const uint4 *src = recs_in + (size_t)__ldg(ids + __ldg(gather + d)) * RW;
+    uint4 *dst = recs_out + (size_t)d * RW;
+    uint4 r[RW];
+#pragma unroll
+    for (int w = 0; w < RW; ++w) r[w] = __ldg(src + w);
+#pragma unroll
+    for (int w = 0; w < RW; ++w) dst[w] = r[w];
 }
 
 // ---------------------------------------------------------------------------
@@ -1023,18 +1128,16 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     CollapseArgs ca;
     ca.n = n;
     ca.width = build_width(bc.flags);
-    ca.rec_words = bc.rec_bytes / 16u;
     ca.capacity = cap;
     ca.root_ref = n >= 2 ? 0u : (kLeafBit | 0u);
-    ca.recs_in = recs;
-    ca.recs_out = reinterpret_cast<uint4 *>(A + h.prim_offset);
-    ca.ids = ids0;
+    ca.gather = ids1;  // free once the sort has left its result in keys0/ids0
     ca.bin = bin;
     ca.node_box = ra.node_box;
     ca.leafable = ra.leafable;
     ca.leaf_box = ra.leaf_box;
     ca.wq = reinterpret_cast<uint32_t *>(S + L.wq);
     ca.slots = reinterpret_cast<uint32_t *>(S + L.slots);
+    ca.desc = reinterpret_cast<uint32_t *>(S + L.desc);
     ca.counts = reinterpret_cast<uint32_t *>(S + L.counts);
     ca.blk = reinterpret_cast<uint32_t *>(S + L.blk);
     ca.nodes_out = reinterpret_cast<uint4 *>(A + h.node_offset);
@@ -1050,6 +1153,12 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     void *args[] = {&ca};
     RT_CUDA_CTX(ctx, cudaLaunchCooperativeKernel((const void *)k_collapse, dim3((unsigned)G),
                                                  dim3(kCollapseThreads), args, 0, st));
+    uint4 *recs_out = reinterpret_cast<uint4 *>(A + h.prim_offset);
+    if (bc.rec_bytes == 48u)
+        k_gather_records<3><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n);
+    else
+        k_gather_records<5><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }
 
