@@ -717,7 +717,10 @@ __device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, 
         sref = __ldcg(a.wq + k);
         src = fetch_ref(a, sref);
     }
-    RefInfo mine = {0u, 0u, 0u, 0u, 0.0f};
+    // mine: this lane's child; pre0/pre1: its binary children, fetched as
+    // soon as the child is known to be openable, so that opening it later
+    // (usually a step or more afterwards) finds them already loaded.
+    RefInfo mine = {0u, 0u, 0u, 0u, 0.0f}, pre0 = mine, pre1 = mine;
     int n = 0;
     if (valid) {
         if (!info_open(src)) {
@@ -728,19 +731,32 @@ __device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, 
             if (j < 2) mine = fetch_ref(a, j == 0 ? src.kid0 : src.kid1);
         }
     }
+    if (valid && j < n && n < (int)a.width && info_open(mine)) {
+        pre0 = fetch_ref(a, mine.kid0);
+        pre1 = fetch_ref(a, mine.kid1);
+    }
     bool act = valid && info_open(src);
     for (;;) {
         act = act && n < (int)a.width;
         if (!__any_sync(kFullMask, act)) break;
         const int best = group_argmax(mine.area, act && j < n && info_open(mine) && mine.area > -1.0f);
         const int from = gb | (best < 0 ? 0 : best);
-        const uint32_t k0 = __shfl_sync(kFullMask, mine.kid0, from);
-        const uint32_t k1 = __shfl_sync(kFullMask, mine.kid1, from);
+        RefInfo moved;
+        moved.ref = __shfl_sync(kFullMask, pre1.ref, from);
+        moved.kid0 = __shfl_sync(kFullMask, pre1.kid0, from);
+        moved.kid1 = __shfl_sync(kFullMask, pre1.kid1, from);
+        moved.cnt = __shfl_sync(kFullMask, pre1.cnt, from);
+        moved.area = __shfl_sync(kFullMask, pre1.area, from);
         if (best < 0) act = false;
         if (act) {
-            if (j == best) mine = fetch_ref(a, k0);
-            else if (j == n) mine = fetch_ref(a, k1);
+            const bool fresh = j == best || j == n;
+            if (j == best) mine = pre0;
+            else if (j == n) mine = moved;
             ++n;
+            if (fresh && n < (int)a.width && info_open(mine)) {
+                pre0 = fetch_ref(a, mine.kid0);
+                pre1 = fetch_ref(a, mine.kid1);
+            }
         }
     }
 
