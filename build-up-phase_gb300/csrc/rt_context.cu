@@ -97,6 +97,11 @@ extern "C" rt_status rt_context_destroy(rt_context *ctx) {
     if (ctx->host_ready) {
         cudaStreamSynchronize(ctx->h2d);
         cudaStreamSynchronize(ctx->d2h);
+        for (int k = 0; k < rt_context::kHostTraceStreams; ++k) {
+            cudaStreamSynchronize(ctx->htr[k]);
+            cudaStreamDestroy(ctx->htr[k]);
+        }
+        cudaEventDestroy(ctx->ev_start);
         for (int s = 0; s < rt_context::kHostSlots; ++s) {
             cudaEventDestroy(ctx->ev_loaded[s]);
             cudaEventDestroy(ctx->ev_traced[s]);

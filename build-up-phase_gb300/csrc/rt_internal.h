@@ -32,10 +32,12 @@ struct rt_context {
     // Host-memory ray API (rt_trace_*_host): two copy streams and, per
     // device slot of the copy ring, the events that order copy in ->
     // traversal -> copy out -> reuse; created on first use.
-    static constexpr int kHostSlots = 3;
+    static constexpr int kHostSlots = 4;
+    static constexpr int kHostTraceStreams = 3;
     bool host_ready = false;
-    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaStream_t h2d = nullptr, d2h = nullptr, htr[kHostTraceStreams] = {};
     cudaEvent_t ev_loaded[kHostSlots] = {}, ev_traced[kHostSlots] = {}, ev_free[kHostSlots] = {};
+    cudaEvent_t ev_start = nullptr;
     uint32_t slot_next = 0;
     const void *host_scratch = nullptr;  // the ring the events above refer to
     uint64_t host_scratch_bytes = 0;

@@ -448,10 +448,15 @@ extern "C" rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t ac
 }
 
 // ---------------------------------------------------------------------------
-// Rays and results in host memory: a ring of three device slots; chunk k is
+// Rays and results in host memory: a ring of four device slots; chunk k is
 // copied in on the context's copy-in stream once its slot's previous results
-// have left, traced on the caller's stream, and copied out on the copy-out
-// stream, so the copies of neighbouring chunks overlap the traversal.
+// have left, traced on one of three trace streams (round robin), and copied
+// out on the copy-out stream.  The copies of neighbouring chunks overlap the
+// traversal, and so do consecutive traversals: a launch ends on its slowest
+// ray (a grazing primary ray walks hundreds of nodes), and the next chunk's
+// launch fills the SMs the finished warps leave.  The first chunk is small
+// (2^18 rays) so the pipeline fills quickly; chunks then double up to what a
+// slot holds.
 // ---------------------------------------------------------------------------
 
 namespace {
@@ -483,6 +488,9 @@ int host_setup(rt_context *ctx) {
     if (ctx->host_ready) return RT_OK;
     RT_CUDA_CTX(ctx, cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
     RT_CUDA_CTX(ctx, cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    for (int k = 0; k < rt_context::kHostTraceStreams; ++k)
+        RT_CUDA_CTX(ctx, cudaStreamCreateWithFlags(&ctx->htr[k], cudaStreamNonBlocking));
+    RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
     for (int s = 0; s < rt_context::kHostSlots; ++s) {
         RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_loaded[s], cudaEventDisableTiming));
         RT_CUDA_CTX(ctx, cudaEventCreateWithFlags(&ctx->ev_traced[s], cudaEventDisableTiming));
@@ -509,26 +517,29 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
     }
     uint8_t *S = static_cast<uint8_t *>(scratch);
     const uint32_t out_size = any ? 1u : 16u;
-    // at least four chunks per call (so that only a quarter of the copies
-    // fill and drain the pipeline), of 2^18 to 2^20 rays
-    uint32_t chunk = (uint32_t)align_up((n + 3u) / 4u, 1024);
-    if (chunk < kHostChunk / 4u) chunk = kHostChunk / 4u;
-    if (chunk > H.chunk) chunk = H.chunk;
-    int s = 0;
-    for (uint32_t off = 0; off < n; off += chunk) {
-        const uint32_t m = n - off < chunk ? n - off : chunk;
+    // everything of the call starts after the work queued on `stream` so far
+    RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_start, st));
+    RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_start, 0));
+    for (int k = 0; k < rt_context::kHostTraceStreams; ++k)
+        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->htr[k], ctx->ev_start, 0));
+    uint32_t chunk = kHostChunk / 4u < H.chunk ? kHostChunk / 4u : H.chunk;
+    int s = 0, k = 0;
+    for (uint32_t off = 0, m = 0; off < n; off += m, ++k) {
+        m = n - off < chunk ? n - off : chunk;
+        chunk = chunk * 2u < H.chunk ? chunk * 2u : H.chunk;
         s = (int)(ctx->slot_next++ % (uint32_t)rt_context::kHostSlots);
+        cudaStream_t ts = ctx->htr[k % rt_context::kHostTraceStreams];
         uint8_t *rays_d = S + (uint64_t)s * H.slot_bytes;
         uint8_t *out_d = rays_d + H.out_offset;
         RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_free[s], 0));
         RT_CUDA_CTX(ctx, cudaMemcpyAsync(rays_d, hrays + off, (size_t)m * 32u, cudaMemcpyHostToDevice, ctx->h2d));
         RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_loaded[s], ctx->h2d));
-        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(st, ctx->ev_loaded[s], 0));
-        rc = launch_batch(ctx, st, accel, reinterpret_cast<const rt_ray *>(rays_d),
+        RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ts, ctx->ev_loaded[s], 0));
+        rc = launch_batch(ctx, ts, accel, reinterpret_cast<const rt_ray *>(rays_d),
                           any ? nullptr : reinterpret_cast<rt_hit *>(out_d), nullptr, any ? out_d : nullptr, m, any,
                           nullptr);
         if (rc) return rc;
-        RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_traced[s], st));
+        RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_traced[s], ts));
         RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->d2h, ctx->ev_traced[s], 0));
         RT_CUDA_CTX(ctx, cudaMemcpyAsync(static_cast<uint8_t *>(hout) + (size_t)off * out_size, out_d,
                                          (size_t)m * out_size, cudaMemcpyDeviceToHost, ctx->d2h));

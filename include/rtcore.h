@@ -340,11 +340,13 @@ rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t accel,
 /*
  * The same traversals with the rays and results in HOST memory (pinned for
  * the copies to overlap): the rays go to the device and the results come
- * back in chunks (a quarter of the call, 2^18 to 2^20 rays, at most what a
- * slot holds) through a ring of three slots in
+ * back in chunks (2^18 rays first, then doubling up to 2^20 or what a slot
+ * holds) through a ring of four slots in
  * `scratch` (rt_trace_host_scratch_bytes(n): enough for chunks of n rays; a
  * smaller scratch means smaller chunks), the copies of neighbouring chunks
- * running on the context's two copy streams while `stream` traces.  Calls that
+ * running on the context's two copy streams and the chunks traced on three
+ * trace streams of the context, so consecutive traversals overlap too.  The
+ * call's work starts after what `stream` holds when it is made.  Calls that
  * share a scratch buffer (closest and any hit alike) overlap each other's
  * copies.  Asynchronous: the results are in host memory when `stream` reaches
  * the end of the call.  The
