@@ -10,7 +10,9 @@ region).  Metric: Mrays/s over both ray sets, inputs resident in HBM.
 
 Prints one JSON line.  Besides the headline value it reports:
   e2e           the same metric through the C ABI with rays in pinned host
-                memory and hits copied back, copies inside the timed region
+                memory and hits returned there: the traversal launch reads
+                the rays and writes the hits over NVLink-C2C inside the
+                timed region (132.7 MB in, 66.4 MB out per step)
   roofline      achieved algorithmic GB/s of the traversal kernel (rays x
                 (48 B ray I/O + 80 B x nodes visited + 36 B x triangles
                 tested), counts from the instrumented kernel) over measured
@@ -371,9 +373,10 @@ def run_ours(args) -> int:
     hp_rays = torch.from_numpy(prim.view(np.uint8)).pin_memory()
     hi_rays = torch.from_numpy(inc.view(np.uint8)).pin_memory()
 
-    # rt_trace_closest_host: the step's rays (primary, then incoherent) in and
-    # its hits out of pinned host memory, in chunks whose copies overlap the
-    # traversal of their neighbours
+    # rt_trace_closest_host: the step's rays (primary, then incoherent) read
+    # from and its hits written to pinned host memory -- in place by the
+    # traversal launch, over NVLink-C2C (the copy path with chunked, overlapped
+    # copies serves pageable buffers)
     h_rays = torch.cat([hp_rays, hi_rays]).pin_memory()
     h_hits = torch.empty(n_all * 16, dtype=torch.uint8).pin_memory()
     hnb = ctx.trace_host_scratch_bytes(n_all)
@@ -382,17 +385,29 @@ def run_ours(args) -> int:
     def e2e_step():
         ctx.trace_closest_host(addr, h_rays, h_hits, n_all, hscratch, hnb, stream)
 
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
+    def e2e_time(k_steps):
+        """ms per call, each call between its own events, L2 flushed between
+        calls outside them (as for the device-resident steps)."""
+        for _ in range(2):
+            e2e_step()
+            flush.fill_(1)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k_steps)]
+        for k in range(k_steps):
+            ev[k][0].record(stream)
+            e2e_step()
+            ev[k][1].record(stream)
+            flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / k_steps
+
     k_e2e = max(3, args.steps)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(k_e2e):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / k_e2e
+    e2e_ms = e2e_time(k_e2e)
+    # the same calls with the rays and hits staged through the scratch ring
+    # (chunked copies on two copy streams, traced on three trace streams)
+    ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_STAGED)
+    e2e_staged_ms = e2e_time(min(k_e2e, 50))
+    ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_AUTO)
     e2e_value = n_all * world / (e2e_ms * 1e-3) / 1e6
 
     extra = secondary_workloads(ctx, stream, dev) if (rank == 0 and not args.no_secondary) else {}
@@ -414,7 +429,13 @@ def run_ours(args) -> int:
                           "l2": "flushed between steps (256 MB write, outside the step events)",
                           "bvh_nodes": n_nodes, "bvh_depth": depth},
                "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",
-                       "h2d_bytes_per_step": n_all * 32, "d2h_bytes_per_step": n_all * 16},
+                       "h2d_bytes_per_step": n_all * 32, "d2h_bytes_per_step": n_all * 16,
+                       "transfer": "rt_trace_closest_host on pinned host buffers: the traversal launch reads "
+                                   "the rays and writes the hits in place over NVLink-C2C",
+                       "staged_value": round(n_all * world / (e2e_staged_ms * 1e-3) / 1e6, 3),
+                       "staged_transfer": "RT_HOST_TRANSFER_STAGED: chunked copies through the scratch ring, "
+                                          "overlapped with the traversal",
+                       "l2": "flushed between calls (256 MB write, outside the call events)"},
                "gpu_launches": 4 * args.steps,
                "roofline": roofline,
                "cpu_baseline": cpu,

@@ -39,6 +39,7 @@ struct rt_context {
     cudaEvent_t ev_loaded[kHostSlots] = {}, ev_traced[kHostSlots] = {}, ev_free[kHostSlots] = {};
     cudaEvent_t ev_start = nullptr;
     uint32_t slot_next = 0;
+    uint32_t host_transfer = 0;  // RT_HOST_TRANSFER_*
     const void *host_scratch = nullptr;  // the ring the events above refer to
     uint64_t host_scratch_bytes = 0;
 };

@@ -448,7 +448,7 @@ extern "C" rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t ac
 }
 
 // ---------------------------------------------------------------------------
-// Rays and results in host memory: a ring of four device slots; chunk k is
+// Rays and results in pageable host memory: a ring of four device slots; chunk k is
 // copied in on the context's copy-in stream once its slot's previous results
 // have left, traced on one of three trace streams (round robin), and copied
 // out on the copy-out stream.  The copies of neighbouring chunks overlap the
@@ -500,13 +500,41 @@ int host_setup(rt_context *ctx) {
     return RT_OK;
 }
 
+// True when the device reaches [p, p + bytes) at the same address: pinned or
+// registered host memory under unified addressing (cudaHostAlloc,
+// cudaHostRegister).  Pageable memory answers false.
+bool device_mapped(const void *p, uint64_t bytes) {
+    const uint8_t *b = static_cast<const uint8_t *>(p);
+    for (const uint8_t *q : {b, b + (bytes ? bytes - 1u : 0u)}) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return false;
+        }
+        if (at.type != cudaMemoryTypeHost || at.devicePointer != q) return false;
+    }
+    return true;
+}
+
 int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *hrays, void *hout, uint32_t n,
                bool any, void *scratch, uint64_t scratch_bytes) {
     if (n == 0) return RT_OK;
+    const uint32_t out_size = any ? 1u : 16u;
+    // Pinned rays and results: one launch reads the rays and writes the
+    // results where they are.  On a Grace-Blackwell system the GPU reaches
+    // that memory coherently over NVLink-C2C; a ray is read once (32 bytes)
+    // and a result written once, so no staging copy, chunk or ring is needed
+    // (4.15M rays of the 1M soup: 2.14 ms, against 2.47 ms for the chunked
+    // copies and 2.07 ms with rays and hits in HBM).
+    RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+    if (ctx->host_transfer == RT_HOST_TRANSFER_AUTO && (reinterpret_cast<uintptr_t>(hrays) & 15u) == 0 &&
+        (any || (reinterpret_cast<uintptr_t>(hout) & 15u) == 0) &&
+        device_mapped(hrays, (uint64_t)n * 32u) && device_mapped(hout, (uint64_t)n * out_size))
+        return launch_batch(ctx, st, accel, hrays, any ? nullptr : static_cast<rt_hit *>(hout), nullptr,
+                            any ? static_cast<uint8_t *>(hout) : nullptr, n, any, nullptr);
     const HostSlots H = host_slots(scratch_bytes);
     if (H.chunk == 0) return set_error(ctx, RT_ERR_OOM, "rt_trace_*_host: scratch smaller than rt_trace_host_scratch_bytes(1)");
     if (reinterpret_cast<uintptr_t>(scratch) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_trace_*_host: scratch must be 256-byte aligned");
-    RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
     int rc = host_setup(ctx);
     if (rc) return rc;
     if (scratch != ctx->host_scratch || scratch_bytes != ctx->host_scratch_bytes) {
@@ -516,7 +544,6 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
         ctx->host_scratch_bytes = scratch_bytes;
     }
     uint8_t *S = static_cast<uint8_t *>(scratch);
-    const uint32_t out_size = any ? 1u : 16u;
     // everything of the call starts after the work queued on `stream` so far
     RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_start, st));
     RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_start, 0));
@@ -551,6 +578,14 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
 }
 
 }  // namespace
+
+extern "C" rt_status rt_set_host_transfer(rt_context *ctx, uint32_t mode) {
+    if (!ctx) return RT_ERR_INVALID_ARG;
+    if (mode != RT_HOST_TRANSFER_AUTO && mode != RT_HOST_TRANSFER_STAGED)
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_set_host_transfer: unknown mode");
+    ctx->host_transfer = mode;
+    return RT_OK;
+}
 
 extern "C" rt_status rt_trace_host_scratch_bytes(uint32_t n, int any_hit, uint64_t *bytes) {
     (void)any_hit;  // one ring serves both kinds of call

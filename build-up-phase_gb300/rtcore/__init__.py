@@ -38,6 +38,8 @@ STATUS_NAMES = {0: "RT_OK", -1: "RT_ERR_INVALID_ARG", -2: "RT_ERR_OOM", -3: "RT_
                 -7: "RT_ERR_NO_DEVICE", -8: "RT_ERR_NOT_FOUND"}
 RT_BUILD_WIDTH_MASK = 0xF << 16
 RT_PT_OCTANT_BINNING = 1
+RT_HOST_TRANSFER_AUTO = 0
+RT_HOST_TRANSFER_STAGED = 1
 RT_BATCH_GRAPH = 1
 RT_BATCH_DISCARD = 2
 RT_TUNE_FORCE = 1
@@ -188,6 +190,7 @@ PROTOTYPES = {
     "rt_trace_any": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32]),
     "rt_generate_primary_rays": (_i32, [_vp, _vp, C.POINTER(Camera), _u32, _u32, _f, _f, _vp]),
     "rt_trace_host_scratch_bytes": (_i32, [_u32, _i32, C.POINTER(_u64)]),
+    "rt_set_host_transfer": (_i32, [_vp, _u32]),
     "rt_trace_closest_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32, _vp, _u64]),
     "rt_trace_any_host": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32, _vp, _u64]),
     "rt_trace_stats": (_i32, [_vp, _vp, _u64, _vp, _u32, _i32, _vp]),
@@ -345,6 +348,9 @@ class Context:
         self.check(self.lib.rt_build_tlas(self.h, _stream_ptr(stream), _ptr(instances), n, flags, _ptr(accel),
                                           accel_bytes, _ptr(scratch), scratch_bytes), "rt_build_tlas")
 
+    def set_host_transfer(self, mode: int) -> None:
+        self.check(self.lib.rt_set_host_transfer(self.h, mode), "rt_set_host_transfer")
+
     def trace_host_scratch_bytes(self, n: int, any_hit: bool = False) -> int:
         out = C.c_uint64()
         self.check(self.lib.rt_trace_host_scratch_bytes(n, 1 if any_hit else 0, C.byref(out)),
@@ -353,8 +359,9 @@ class Context:
 
     def trace_closest_host(self, accel_addr: int, rays, hits, n: int, scratch, scratch_bytes: int,
                            stream=None) -> None:
-        """rays / hits: host buffers (torch CPU tensors, pinned for overlap, or
-        raw addresses)."""
+        """rays / hits: host buffers (torch CPU tensors or raw addresses);
+        pinned ones are read and written in place by the traversal launch,
+        pageable ones go through the scratch ring in chunks."""
         self.check(self.lib.rt_trace_closest_host(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(hits), n,
                                                   _ptr(scratch), scratch_bytes), "rt_trace_closest_host")
 

@@ -84,6 +84,26 @@ def test_blas_duplicates_degenerates_and_bad_indices(ctx, orc):
     assert rc2 == rtcore.RT_ERR_BOUNDS
 
 
+@pytest.mark.parametrize("seed,frac", [(1, 1.0), (3, 1.0), (7, 0.5), (11, 0.5)])
+def test_blas_extreme_coordinates_bit_exact(ctx, orc, seed, frac):
+    """Vertices at +-1e30..3e38 mixed with unit-cube ones: box centres
+    overflow, so some octant-slot costs are inf - inf = NaN.  These seeds
+    make the slot assignment meet a NaN both as the first (child, slot) pair
+    of a round -- which the sequential scan then keeps -- and after it (where
+    it never wins); the eight-lane assignment must make the same choices."""
+    rng = np.random.default_rng(seed)
+    big = np.array([-3.0e38, -1.7e38, -1e30, 1e30, 1.7e38, 3.0e38], np.float32)
+    nb = int(600 * frac)
+    v = np.concatenate([rng.choice(big, size=(nb * 3, 3)).astype(np.float32),
+                        rng.uniform(0, 1, size=((600 - nb) * 3, 3)).astype(np.float32)])
+    idx = rng.permutation(len(v)).astype(np.uint32).reshape(-1, 3)
+    items = [(v, idx, None)]
+    g = GpuBlas(ctx, items)
+    o, rc = orc.build_blas(items)
+    assert rc == 0
+    compare_accels(g.bytes(), o, 48)
+
+
 def test_blas_box_scene_bit_exact(ctx, orc):
     import rtcore.scenes as S
     v, i, tm, m = S.box(S.SEED_BASE + 3, 6, 12)

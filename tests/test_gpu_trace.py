@@ -268,8 +268,9 @@ def test_rt_sample_obj_mesh(rtlib, orc, tmp_path):
 @pytest.mark.parametrize("n", [0, 1, 1000, (1 << 20) + 12345, 3 * (1 << 20) + 1])
 def test_host_memory_rays(ctx, orc, n):
     """rt_trace_closest_host / rt_trace_any_host (rays and results in host
-    memory, chunked copies overlapping the traversal) give the device API's
-    results, from pinned and from pageable buffers, over repeated calls."""
+    memory: read and written in place when pinned, chunked copies overlapping
+    the traversal when pageable) give the device API's results, over repeated
+    calls; a pinned buffer at an odd offset takes the copy path."""
     import torch
     import rtcore.scenes as S
     items = soup(50_000, seed=3)
@@ -292,6 +293,54 @@ def test_host_memory_rays(ctx, orc, n):
         if n:
             assert hh.numpy()[:n * 16].tobytes() == want.tobytes()
             assert ho.numpy()[:n].tobytes() == want_occ.tobytes()
+    if n:
+        # pinned buffers forced through the staged (copy) path
+        import rtcore
+        ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_STAGED)
+        try:
+            hr = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+            hh = torch.full((n * 16,), 0xAB, dtype=torch.uint8).pin_memory()
+            ctx.trace_closest_host(g.addr, hr, hh, n, scratch, nb)
+            ctx.sync()
+            assert hh.numpy().tobytes() == want.tobytes()
+            with pytest.raises(rtcore.RtError) as e:
+                ctx.set_host_transfer(7)
+            assert e.value.code == rtcore.RT_ERR_INVALID_ARG
+        finally:
+            ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_AUTO)
+        # pinned but not 16-byte aligned: rays and hits one byte into their buffers
+        hr1 = torch.zeros(n * 32 + 16, dtype=torch.uint8).pin_memory()
+        hr1[1:1 + n * 32] = torch.from_numpy(rays.view(np.uint8).copy())
+        hh1 = torch.full((n * 16 + 16,), 0xAB, dtype=torch.uint8).pin_memory()
+        ctx.trace_closest_host(g.addr, hr1.data_ptr() + 1, hh1.data_ptr() + 1, n, scratch, nb)
+        ctx.sync()
+        assert hh1.numpy()[1:1 + n * 16].tobytes() == want.tobytes()
+
+
+def test_host_memory_rays_small_scratch(ctx, orc):
+    """Pageable buffers (the copy path) and a scratch sized for 5,000-ray
+    chunks: 200,003 rays go round the four-slot ring in 41 chunks on three
+    trace streams, closest and any-hit calls alternating on one scratch;
+    results equal the device API's."""
+    import torch
+    import rtcore.scenes as S
+    n = 200_003
+    items = soup(50_000, seed=5)
+    g = GpuBlas(ctx, items)
+    rays = S.incoherent_rays(91, n, (0, 0, 0), (1, 1, 1), 1e30)
+    want = gpu_trace_closest(ctx, g.addr, rays)
+    want_occ = gpu_trace_any(ctx, g.addr, rays)
+    nb = ctx.trace_host_scratch_bytes(5000)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    hr = torch.from_numpy(rays.view(np.uint8).copy())
+    hh = torch.full((n * 16,), 0xAB, dtype=torch.uint8)
+    ho = torch.full((n,), 7, dtype=torch.uint8)
+    for _ in range(3):
+        ctx.trace_closest_host(g.addr, hr, hh, n, scratch, nb)
+        ctx.trace_any_host(g.addr, hr, ho, n, scratch, nb)
+    ctx.sync()
+    assert hh.numpy().tobytes() == want.tobytes()
+    assert ho.numpy().tobytes() == want_occ.tobytes()
 
 
 def test_full_size_soup_sampled(ctx, orc):
