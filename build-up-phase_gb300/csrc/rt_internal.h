@@ -40,6 +40,7 @@ struct rt_context {
     cudaEvent_t ev_start = nullptr;
     uint32_t slot_next = 0;
     uint32_t host_transfer = 0;  // RT_HOST_TRANSFER_*
+    int pageable_state = 0;      // 0 not queried, 1 pageable memory reachable in place, 2 not
     const void *host_scratch = nullptr;  // the ring the events above refer to
     uint64_t host_scratch_bytes = 0;
 };

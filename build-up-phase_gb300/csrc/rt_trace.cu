@@ -448,7 +448,9 @@ extern "C" rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t ac
 }
 
 // ---------------------------------------------------------------------------
-// Rays and results in pageable host memory: a ring of four device slots; chunk k is
+// Rays and results staged through the scratch (pageable memory the device
+// cannot reach, misaligned buffers, RT_HOST_TRANSFER_STAGED): a ring of four
+// device slots; chunk k is
 // copied in on the context's copy-in stream once its slot's previous results
 // have left, traced on one of three trace streams (round robin), and copied
 // out on the copy-out stream.  The copies of neighbouring chunks overlap the
@@ -500,10 +502,13 @@ int host_setup(rt_context *ctx) {
     return RT_OK;
 }
 
-// True when the device reaches [p, p + bytes) at the same address: pinned or
+// True when kernels reach [p, p + bytes) at the same address: pinned or
 // registered host memory under unified addressing (cudaHostAlloc,
-// cudaHostRegister).  Pageable memory answers false.
-bool device_mapped(const void *p, uint64_t bytes) {
+// cudaHostRegister), device or managed memory, and -- where the device
+// accesses pageable memory through the host's page tables (a Grace system's
+// NVLink-C2C; `pageable` from the device attributes) -- plain pageable
+// memory.
+bool reachable_in_place(const void *p, uint64_t bytes, bool pageable) {
     const uint8_t *b = static_cast<const uint8_t *>(p);
     for (const uint8_t *q : {b, b + (bytes ? bytes - 1u : 0u)}) {
         cudaPointerAttributes at;
@@ -511,25 +516,47 @@ bool device_mapped(const void *p, uint64_t bytes) {
             (void)cudaGetLastError();
             return false;
         }
-        if (at.type != cudaMemoryTypeHost || at.devicePointer != q) return false;
+        if (at.type == cudaMemoryTypeHost) {
+            if (at.devicePointer != q) return false;
+        } else if (at.type == cudaMemoryTypeUnregistered) {
+            if (!pageable) return false;
+        }
     }
     return true;
+}
+
+// Whether the context's device reads and writes pageable host memory
+// coherently through the host page tables (queried once).
+bool pageable_in_place(rt_context *ctx) {
+    if (ctx->pageable_state == 0) {
+        int a = 0, b = 0;
+        const bool ok = cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, ctx->device) == cudaSuccess &&
+                        cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) ==
+                            cudaSuccess;
+        (void)cudaGetLastError();
+        ctx->pageable_state = (ok && a == 1 && b == 1) ? 1 : 2;
+    }
+    return ctx->pageable_state == 1;
 }
 
 int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *hrays, void *hout, uint32_t n,
                bool any, void *scratch, uint64_t scratch_bytes) {
     if (n == 0) return RT_OK;
     const uint32_t out_size = any ? 1u : 16u;
-    // Pinned rays and results: one launch reads the rays and writes the
-    // results where they are.  On a Grace-Blackwell system the GPU reaches
-    // that memory coherently over NVLink-C2C; a ray is read once (32 bytes)
-    // and a result written once, so no staging copy, chunk or ring is needed
-    // (4.15M rays of the 1M soup: 2.14 ms, against 2.47 ms for the chunked
-    // copies and 2.07 ms with rays and hits in HBM).
+    // Rays and results the kernels reach in place (pinned memory; on a
+    // Grace-Blackwell system also pageable memory, through the host page
+    // tables): one launch reads the rays and writes the results where they
+    // are, over NVLink-C2C.  A ray is read once (32 bytes) and a result
+    // written once, so no staging copy, chunk or ring is needed (4.15M rays
+    // of the 1M soup: 2.14 ms pinned or pageable, against 2.47 ms staged from
+    // pinned, 3.91 ms staged from pageable and 2.07 ms with rays and hits in
+    // HBM).
     RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+    const bool pageable = pageable_in_place(ctx);
     if (ctx->host_transfer == RT_HOST_TRANSFER_AUTO && (reinterpret_cast<uintptr_t>(hrays) & 15u) == 0 &&
         (any || (reinterpret_cast<uintptr_t>(hout) & 15u) == 0) &&
-        device_mapped(hrays, (uint64_t)n * 32u) && device_mapped(hout, (uint64_t)n * out_size))
+        reachable_in_place(hrays, (uint64_t)n * 32u, pageable) &&
+        reachable_in_place(hout, (uint64_t)n * out_size, pageable))
         return launch_batch(ctx, st, accel, hrays, any ? nullptr : static_cast<rt_hit *>(hout), nullptr,
                             any ? static_cast<uint8_t *>(hout) : nullptr, n, any, nullptr);
     const HostSlots H = host_slots(scratch_bytes);

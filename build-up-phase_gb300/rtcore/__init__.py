@@ -360,8 +360,9 @@ class Context:
     def trace_closest_host(self, accel_addr: int, rays, hits, n: int, scratch, scratch_bytes: int,
                            stream=None) -> None:
         """rays / hits: host buffers (torch CPU tensors or raw addresses);
-        pinned ones are read and written in place by the traversal launch,
-        pageable ones go through the scratch ring in chunks."""
+        read and written in place by the traversal launch where the device
+        reaches them (pinned memory; pageable memory on a Grace system), else
+        staged through the scratch ring in chunks."""
         self.check(self.lib.rt_trace_closest_host(self.h, _stream_ptr(stream), accel_addr, _ptr(rays), _ptr(hits), n,
                                                   _ptr(scratch), scratch_bytes), "rt_trace_closest_host")
 

@@ -340,11 +340,13 @@ rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t accel,
 /*
  * The same traversals with the rays and results in HOST memory (pinned for
  * the copies to overlap): the rays go to the device and the results come
- * back.  When both buffers are pinned or registered host memory that the
- * device maps at the same address (cudaHostAlloc / cudaHostRegister under
- * unified addressing) and 16-byte aligned, one traversal launch reads the
- * rays and writes the results in place -- on a Grace-Blackwell system over
- * NVLink-C2C -- and `scratch` is not touched.  Otherwise the rays go in and
+ * back.  When both buffers are 16-byte aligned and the device reaches them
+ * at the same address -- pinned or registered host memory under unified
+ * addressing (cudaHostAlloc / cudaHostRegister), or any host memory on a
+ * device that accesses pageable memory through the host page tables (a
+ * Grace-Blackwell system, over NVLink-C2C) -- one traversal launch reads the
+ * rays and writes the results in place and `scratch` is not touched.
+ * Otherwise the rays go in and
  * the results come back in chunks (2^18 rays first, then doubling up to 2^20
  * or what a slot holds) through a ring of four slots in
  * `scratch` (rt_trace_host_scratch_bytes(n): enough for chunks of n rays; a
@@ -360,8 +362,9 @@ rt_status rt_trace_any(rt_context *ctx, rt_stream stream, uint64_t accel,
  */
 rt_status rt_trace_host_scratch_bytes(uint32_t n, int any_hit, uint64_t *bytes);
 /* How the host-memory calls move rays and results: RT_HOST_TRANSFER_AUTO
- * (default) reads and writes pinned buffers in place and stages the others
- * through the scratch ring; RT_HOST_TRANSFER_STAGED always stages. */
+ * (default) reads and writes the buffers in place where the device reaches
+ * them and stages the others through the scratch ring;
+ * RT_HOST_TRANSFER_STAGED always stages. */
 enum { RT_HOST_TRANSFER_AUTO = 0, RT_HOST_TRANSFER_STAGED = 1 };
 rt_status rt_set_host_transfer(rt_context *ctx, uint32_t mode);
 rt_status rt_trace_closest_host(rt_context *ctx, rt_stream stream, uint64_t accel, const rt_ray *rays,

@@ -268,9 +268,11 @@ def test_rt_sample_obj_mesh(rtlib, orc, tmp_path):
 @pytest.mark.parametrize("n", [0, 1, 1000, (1 << 20) + 12345, 3 * (1 << 20) + 1])
 def test_host_memory_rays(ctx, orc, n):
     """rt_trace_closest_host / rt_trace_any_host (rays and results in host
-    memory: read and written in place when pinned, chunked copies overlapping
-    the traversal when pageable) give the device API's results, over repeated
-    calls; a pinned buffer at an odd offset takes the copy path."""
+    memory: read and written in place where the device reaches them -- pinned,
+    and pageable on a Grace system -- else chunked copies overlapping the
+    traversal) give the device API's results, over repeated calls; pinned
+    buffers forced to the staged path and a pinned buffer at an odd offset
+    (staged) as well."""
     import torch
     import rtcore.scenes as S
     items = soup(50_000, seed=3)
@@ -318,10 +320,10 @@ def test_host_memory_rays(ctx, orc, n):
 
 
 def test_host_memory_rays_small_scratch(ctx, orc):
-    """Pageable buffers (the copy path) and a scratch sized for 5,000-ray
-    chunks: 200,003 rays go round the four-slot ring in 41 chunks on three
-    trace streams, closest and any-hit calls alternating on one scratch;
-    results equal the device API's."""
+    """The staged path (RT_HOST_TRANSFER_STAGED) from pageable buffers with a
+    scratch sized for 5,000-ray chunks: 200,003 rays go round the four-slot
+    ring in 41 chunks on three trace streams, closest and any-hit calls
+    alternating on one scratch; results equal the device API's."""
     import torch
     import rtcore.scenes as S
     n = 200_003
@@ -335,10 +337,15 @@ def test_host_memory_rays_small_scratch(ctx, orc):
     hr = torch.from_numpy(rays.view(np.uint8).copy())
     hh = torch.full((n * 16,), 0xAB, dtype=torch.uint8)
     ho = torch.full((n,), 7, dtype=torch.uint8)
-    for _ in range(3):
-        ctx.trace_closest_host(g.addr, hr, hh, n, scratch, nb)
-        ctx.trace_any_host(g.addr, hr, ho, n, scratch, nb)
-    ctx.sync()
+    import rtcore
+    ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_STAGED)
+    try:
+        for _ in range(3):
+            ctx.trace_closest_host(g.addr, hr, hh, n, scratch, nb)
+            ctx.trace_any_host(g.addr, hr, ho, n, scratch, nb)
+        ctx.sync()
+    finally:
+        ctx.set_host_transfer(rtcore.RT_HOST_TRANSFER_AUTO)
     assert hh.numpy().tobytes() == want.tobytes()
     assert ho.numpy().tobytes() == want_occ.tobytes()
 
