@@ -70,6 +70,9 @@ inline void camera_aspects(const rt_camera *cam, uint32_t w, uint32_t h, float *
 // Queue-driven BLAS traversal (rt_trace.cu) used by the path tracer.
 int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
                        uint8_t *occluded, const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any);
+int launch_queue_trace_mixed(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
+                             const uint32_t *n_dev, const void *rays2, uint8_t *occluded, const uint32_t *n_dev2,
+                             uint32_t max_n, uint32_t *counter);
 
 // Launch shape of the multi-scene traversal (rt_trace_multi.cu).
 struct TraceShape {
@@ -86,6 +89,11 @@ int launch_queue_trace_multi(rt_context *ctx, cudaStream_t st, const void *views
                              const uint32_t *ray_scene, const void *rays, void *hits, uint8_t *occluded,
                              const uint32_t *n_dev, uint32_t max_n, uint32_t *counter, bool any,
                              const TraceShape &shape);
+int launch_queue_trace_multi_mixed(rt_context *ctx, cudaStream_t st, const void *views, uint32_t n_scenes,
+                                   const uint32_t *ray_scene, const void *rays, void *hits, const uint32_t *n_dev,
+                                   const uint32_t *ray_scene2, const void *rays2, uint8_t *occluded,
+                                   const uint32_t *n_dev2, uint32_t max_n, uint32_t *counter,
+                                   const TraceShape &shape);
 
 // Loads the two traversal kernels of a shape (before a graph capture).
 int prepare_queue_trace_multi(rt_context *ctx, const TraceShape &shape);

@@ -806,11 +806,14 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
                                                    p->camera.position[2], p->width, p->height, p->seed, sample_dev,
                                                    rays[0], pidx[0], a.tput, a.rad, a.rng, &cnt[0], ray_counts);
         RT_CUDA_CTX(ctx, cudaGetLastError());
+        // depth 0's extension rays alone; afterwards each launch traces a
+        // depth's shadow rays together with the next depth's extension rays
+        int rc0 = launch_queue_trace(ctx, st, accel, rays[0], S + L.hits, nullptr, &cnt[0], (uint32_t)npix, &tcnt[0],
+                                     false);
+        if (rc0) return rc0;
         for (uint32_t d = 0; d < p->max_depth; ++d) {
             const uint32_t q = d & 1u;
-            int rc = launch_queue_trace(ctx, st, accel, rays[q], S + L.hits, nullptr, &cnt[d], (uint32_t)npix,
-                                        &tcnt[2 * d], false);
-            if (rc) return rc;
+            int rc = RT_OK;
             a.rays_in = rays[q];
             a.pidx_in = pidx[q];
             a.rays_out = rays[q ^ 1u];
@@ -828,8 +831,9 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
                     pidx[q ^ 1u], nullptr, (uint32_t)npix, ctx->d_err);
                 RT_CUDA_CTX(ctx, cudaGetLastError());
             }
-            rc = launch_queue_trace(ctx, st, accel, a.srays, nullptr, socc, &scnt[d], (uint32_t)npix,
-                                    &tcnt[2 * d + 1], true);
+            // cnt[max_depth] stays 0: the last launch traces shadow rays only
+            rc = launch_queue_trace_mixed(ctx, st, accel, rays[q ^ 1u], S + L.hits, &cnt[d + 1], a.srays, socc,
+                                          &scnt[d], (uint32_t)npix, &tcnt[2 * d + 1]);
             if (rc) return rc;
             k_pt_resolve<<<resolve_blocks, kPtThreads, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
             RT_CUDA_CTX(ctx, cudaGetLastError());
@@ -1096,12 +1100,15 @@ int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
             ++k;
             RT_CUDA_CTX(ctx, cudaGetLastError());
             a.wave_base = base;
+            // depth 0's extension rays alone; afterwards each launch traces a
+            // depth's shadow rays together with the next depth's extension rays
+            int rc0 = launch_queue_trace_multi(ctx, st, views, n_sc, rsid[0], rays[0], S + L.hits, nullptr, &cnt[0], n,
+                                               &tcnt[0], false, shape);
+            if (rc0) return rc0;
+            ++k;
             for (uint32_t d = 0; d < pl->p.max_depth; ++d) {
                 const uint32_t q = d & 1u;
-                int rc = launch_queue_trace_multi(ctx, st, views, n_sc, rsid[q], rays[q], S + L.hits, nullptr, &cnt[d],
-                                                  n, &tcnt[2 * d], false, shape);
-                if (rc) return rc;
-                ++k;
+                int rc = RT_OK;
                 a.rays_in = rays[q];
                 a.pidx_in = pidx[q];
                 a.rsid_in = rsid[q];
@@ -1123,8 +1130,10 @@ int batch_enqueue(rt_batch_plan *pl, cudaStream_t st, uint32_t *kernels) {
                     ++k;
                     RT_CUDA_CTX(ctx, cudaGetLastError());
                 }
-                rc = launch_queue_trace_multi(ctx, st, views, n_sc, a.ssid, a.srays, nullptr, socc, &scnt[d], n,
-                                              &tcnt[2 * d + 1], true, shape);
+                // cnt[max_depth] stays 0: the last launch traces shadow rays only
+                rc = launch_queue_trace_multi_mixed(ctx, st, views, n_sc, rsid[q ^ 1u], rays[q ^ 1u], S + L.hits,
+                                                    &cnt[d + 1], a.ssid, a.srays, socc, &scnt[d], n, &tcnt[2 * d + 1],
+                                                    shape);
                 if (rc) return rc;
                 ++k;
                 k_pt_resolve<<<resolve_blocks, T, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
@@ -1288,7 +1297,7 @@ extern "C" rt_status rt_batch_plan_create(rt_context *ctx, const rt_batch_scene 
     } else {
         // count the launches of one direct enqueue without issuing it
         const uint64_t waves = P ? (P + cap - 1u) / cap : 0u;
-        const uint64_t per_wave = 2u + 4u * p->max_depth + ((p->flags & RT_PT_OCTANT_BINNING) ? p->max_depth - 1u : 0u);
+        const uint64_t per_wave = 3u + 3u * p->max_depth + ((p->flags & RT_PT_OCTANT_BINNING) ? p->max_depth - 1u : 0u);
         pl->kernels = P ? (uint32_t)(2u + (uint64_t)p->spp * waves * per_wave) : 0u;
     }
     *plan = pl;

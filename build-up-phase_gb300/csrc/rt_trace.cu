@@ -425,6 +425,37 @@ int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, c
     return RT_OK;
 }
 
+// One launch over two queues of at most max_n rays each: closest hits for
+// rays/n_dev (leaf-record index out, to hits), then any hits for
+// rays2/n_dev2 (to occluded).  Capturable like launch_queue_trace.
+int launch_queue_trace_mixed(rt_context *ctx, cudaStream_t st, const uint8_t *accel, const void *rays, void *hits,
+                             const uint32_t *n_dev, const void *rays2, uint8_t *occluded, const uint32_t *n_dev2,
+                             uint32_t max_n, uint32_t *counter) {
+    if (max_n == 0) return RT_OK;
+    BatchArgs a{};
+    a.accel = accel;
+    a.rays = static_cast<const float4 *>(rays);
+    a.hits = static_cast<float4 *>(hits);
+    a.occluded = occluded;
+    a.n = max_n;
+    a.n_dev = n_dev;
+    a.rays2 = static_cast<const float4 *>(rays2);
+    a.n_dev2 = n_dev2;
+    a.n2 = max_n;
+    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 4u;
+    if (a.refill > 32u) a.refill = 32u;
+    a.err = ctx->d_err;
+    a.out_rec = 1;
+    a.counter = counter;
+    uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
+    uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
+    const uint32_t need = (uint32_t)(((uint64_t)max_n * 2u + kTraceThreads - 1) / kTraceThreads);
+    if (blocks > need) blocks = need;
+    k_trace_blas<false, false, false, kTraceThreads, kRing, true><<<blocks, kTraceThreads, 0, st>>>(a);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
+
 namespace {
 
 

@@ -71,9 +71,20 @@ struct BatchArgs {
     unsigned long long *stats;
     const uint32_t *n_dev;   // when set: the ray count, read on the device
     uint32_t out_rec;        // closest hit: write the leaf-record index
+    // mixed launches: a second queue of any-hit rays after the closest-hit
+    // queue above (rays2[i] is ray n1 + i of the launch; results to occluded)
+    const float4 *rays2;
+    const uint32_t *ray_scene2;
+    const uint32_t *n_dev2;
+    uint32_t n2;
 };
 
-template <bool ANY, bool STATS, bool MULTI, int THREADS, int RING>
+// MIXED: one launch over two queues -- the closest-hit rays (rays, n_dev;
+// results to hits) and then the any-hit rays (rays2, n_dev2; results to
+// occluded) -- each ray walked exactly as in a launch of its own kind; the
+// path tracer traces a depth's shadow rays and the next depth's extension
+// rays together, so the two share one launch tail.
+template <bool ANY, bool STATS, bool MULTI, int THREADS, int RING, bool MIXED = false>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const BatchArgs a) {
     static_assert((RING & (RING - 1)) == 0 && RING <= kMaxDepth, "RING is a power of two");
     __shared__ uint2 s_stack[RING][THREADS];
@@ -105,7 +116,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const Ba
     uint2 spill[kMaxDepth];
     unsigned long long n_nodes = 0, n_tris = 0;
     uint32_t visits = 0;
-    const uint32_t n_rays = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const uint32_t n1 = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const uint32_t n_rays = MIXED ? n1 + min(*a.n_dev2, a.n2) : n1;
+    bool any_ray = ANY;  // this lane's ray is an any-hit ray
 
     for (;;) {
         // ---- refill idle lanes from the global counter
@@ -117,10 +130,20 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const Ba
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base + cnt >= n_rays) exhausted = true;
             if (!active) {
-                const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+                uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
                 if (idx < n_rays) {
+                    const float4 *ray_src = a.rays;
+                    const uint32_t *scene_src = a.ray_scene;
+                    if (MIXED) {
+                        any_ray = idx >= n1;
+                        if (any_ray) {
+                            idx -= n1;
+                            ray_src = a.rays2;
+                            scene_src = a.ray_scene2;
+                        }
+                    }
                     if (MULTI) {
-                        const uint32_t s = __ldg(a.ray_scene + idx);
+                        const uint32_t s = __ldg(scene_src + idx);
                         if (s < a.n_scenes) {
                             const uint4 *tv = reinterpret_cast<const uint4 *>(a.scenes + s);
                             const uint4 t0 = ldg4(tv), t1 = ldg4(tv + 1);
@@ -133,7 +156,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const Ba
                             empty = true;
                         }
                     }
-                    const float4 r0 = __ldg(a.rays + 2u * idx), r1 = __ldg(a.rays + 2u * idx + 1u);
+                    const float4 r0 = __ldg(ray_src + 2u * idx), r1 = __ldg(ray_src + 2u * idx + 1u);
                     const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
                     ray_setup(r, o, d);
                     tmin = r0.w;
@@ -186,7 +209,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const Ba
                                                    __uint_as_float(q2.z), 0.f),
                                        tmin, h.t, t, u, v))
                             continue;
-                        if (ANY) {
+                        if (ANY || (MIXED && any_ray)) {
                             h.t = t; h.found = true;
                             finish = true;
                             break;
@@ -231,7 +254,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const Ba
                 }
                 if (finish) {
                     // ---- write the result
-                    if (ANY) {
+                    if (ANY || (MIXED && any_ray)) {
                         if (a.occluded) a.occluded[ray_idx] = h.found ? 1u : 0u;
                     } else {
                         float4 out;
