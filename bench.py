@@ -4,7 +4,9 @@ Workload (one "step"): closest-hit traversal of 1920x1080 coherent primary
 rays plus 1920x1080 incoherent rays (origins uniform in the unit cube,
 directions uniform on the sphere) against a seeded soup of 1,000,000 FP32
 triangles in the unit cube (LBVH -> BVH8 built once, outside the timed
-region).  Metric: Mrays/s over both ray sets, inputs resident in HBM.
+region), submitted as one rt_trace_closest call over the step's 4.15M rays
+(primary, then incoherent).  Metric: Mrays/s over both ray sets, inputs
+resident in HBM.  The breakdown times each ray set in a launch of its own.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -58,9 +60,9 @@ BYTES_TRI = 36      # FP32 vertex triplet
 # 24 per sort pass (8 passes of 63-bit keys), 2 x 24 for the radix tree and
 # its refit, 80 / 8 for the BVH8 node share of one leaf-equivalent
 BYTES_BUILD_PER_TRI = 48 + 12 + 24 * 8 + 2 * 24 + 80 // 8
-# DRAM bytes (read + write) of one step's two traversal launches measured by
-# ncu (cold caches): 97.5 MB primary + 392.0 MB incoherent
-TRAFFIC_BYTES_PER_STEP = 489_500_000
+# DRAM bytes (read + write) of one step's traversal launch measured by ncu
+# (cold caches): 424.4 MB read + 66.1 MB written
+TRAFFIC_BYTES_PER_STEP = 490_500_000
 
 
 def _env_int(name: str, default: int) -> int:
@@ -298,22 +300,30 @@ def run_ours(args) -> int:
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
+    # the step's rays in one array: one call traces the whole batch
+    rays_all = torch.cat([rays_p, rays_i])
+    hits_all = torch.empty(n_all * 16, dtype=torch.uint8, device=dev)
+
     def step(ev=None):
         if ev:
             ev[0].record(stream)
-        ctx.trace_closest(addr, rays_p, hits_p, n_p, stream=stream)
+        ctx.trace_closest(addr, rays_all, hits_all, n_all, stream=stream)
         if ev:
             ev[1].record(stream)
+
+    def step_split(ev):
+        ev[0].record(stream)
+        ctx.trace_closest(addr, rays_p, hits_p, n_p, stream=stream)
+        ev[1].record(stream)
         ctx.trace_closest(addr, rays_i, hits_i, n_i, stream=stream)
-        if ev:
-            ev[2].record(stream)
+        ev[2].record(stream)
 
     for _ in range(max(3, args.warmup)):
         step()
         flush.fill_(1)
     ctx.sync(stream)
 
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
     if dist:
         tdist.barrier()
     torch.cuda.synchronize()
@@ -327,19 +337,27 @@ def run_ours(args) -> int:
     if dist:
         tdist.barrier()
     ctx.sync(stream)
-    t_p = [e[0].elapsed_time(e[1]) for e in evs]
-    t_i = [e[1].elapsed_time(e[2]) for e in evs]
-    ms_step = (sum(t_p) + sum(t_i)) / args.steps
+    ms_step = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
     ms_step, value = whole_job(ms_step, n_all, world, dev if dist else None)
 
-    # ---- roofline of the traversal kernel (both launches of the step)
+    # ---- breakdown: each ray set in a launch of its own (L2 flushed between steps)
+    k_split = min(args.steps, 50)
+    evs_s = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(k_split)]
+    for k in range(k_split):
+        step_split(evs_s[k])
+        flush.fill_(k & 0xFF)
+    ctx.sync(stream)
+    t_p = [e[0].elapsed_time(e[1]) for e in evs_s]
+    t_i = [e[1].elapsed_time(e[2]) for e in evs_s]
+
+    # ---- roofline of the traversal kernel (the step's launch)
     peaks = _peaks()
     alg_bytes = n_p * bytes_p + n_i * bytes_i
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4),
-                # dram__bytes_read.sum + dram__bytes_write.sum of the two
-                # launches of one step, from one ncu capture of this workload
+                # dram__bytes_read.sum + dram__bytes_write.sum of the step's
+                # launch, from one ncu capture of this workload
                 # (cold caches): profiles/k_trace_blas_soup1M_1920x1080.md
                 "traffic": TRAFFIC_BYTES_PER_STEP,
                 "algorithmic_bytes_per_step": round(alg_bytes),
@@ -436,11 +454,12 @@ def run_ours(args) -> int:
                        "staged_transfer": "RT_HOST_TRANSFER_STAGED: chunked copies through the scratch ring, "
                                           "overlapped with the traversal",
                        "l2": "flushed between calls (256 MB write, outside the call events)"},
-               "gpu_launches": 4 * args.steps,
+               "gpu_launches": 2 * args.steps,
                "roofline": roofline,
                "cpu_baseline": cpu,
-               "breakdown": {"primary_mrays": round(n_p * args.steps / (sum(t_p) * 1e-3) / 1e6, 2),
-                             "incoherent_mrays": round(n_i * args.steps / (sum(t_i) * 1e-3) / 1e6, 2),
+               "breakdown": {"primary_mrays": round(n_p * k_split / (sum(t_p) * 1e-3) / 1e6, 2),
+                             "incoherent_mrays": round(n_i * k_split / (sum(t_i) * 1e-3) / 1e6, 2),
+                             "separate_launches_mrays": round(n_all * k_split / ((sum(t_p) + sum(t_i)) * 1e-3) / 1e6, 2),
                              "shadow_anyhit_mrays": round(shadow_mrays, 2),
                              "build_ms": round(statistics.median(build_ms), 3),
                              "build_roofline": {
