@@ -34,4 +34,4 @@ def test_oracle_gradient_equals_autograd():
     lt = ((y - tt) ** 2 / den).mean()
     lt.backward()
     np.testing.assert_allclose(g, pt.grad.numpy(), rtol=1e-9, atol=1e-12)
-    assert abs(loss - float(lt)) < 1e-12
+    assert abs(loss - float(lt.detach())) < 1e-12
