@@ -48,7 +48,22 @@ struct PtLayout {
     // learned form: cache queries at the second vertex and training samples
     uint64_t qin, qout, qt1, qpidx, tin, ttarget, tt1, tlpre, tpidx;
     uint32_t cap, train_cap;
+    uint32_t wave;  // samples of every pixel traced together (cap = pixels x wave)
 };
+
+// Samples per pixel traced as one wave by the plain path tracer: a wave of
+// k samples has k times the rays per traversal launch, so each launch's
+// slow-ray tail is shared by k samples.  At most 4, and at most 2^23 paths
+// (~1.9 GB of path state and queues); the learned form keeps one sample per
+// wave (its training pixels are chosen per sample).
+constexpr uint32_t kPtWaveSamples = 4;
+constexpr uint64_t kPtWavePaths = 1ull << 23;
+inline uint32_t wave_samples(uint64_t npix, uint32_t spp, bool cached) {
+    if (cached) return 1u;
+    uint64_t k = spp < kPtWaveSamples ? spp : kPtWaveSamples;
+    while (k > 1u && npix * k > kPtWavePaths) --k;
+    return (uint32_t)(k ? k : 1u);
+}
 
 // counter words of the scratch counter block
 // Counter block (32-bit words): [0, 65) extension queue lengths per depth,
@@ -64,7 +79,9 @@ constexpr uint32_t kCntWords = 800;
 
 PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap = 0) {
     PtLayout L;
-    uint64_t cap = (uint64_t)p.width * p.height;
+    const uint64_t npix = (uint64_t)p.width * p.height;
+    L.wave = wave_samples(npix, p.spp, train_cap > 0);
+    const uint64_t cap = npix * L.wave;
     L.cap = (uint32_t)cap;
     uint64_t off = 0;
     auto take = [&](uint64_t b) {
@@ -72,6 +89,7 @@ PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap 
         off += align_up(b ? b : 1, 256);
         return o;
     };
+    L.counters = take(kCntWords * 4u);  // first: its offset depends on nothing
     L.rays0 = take(cap * 32u);
     L.rays1 = take(cap * 32u);
     L.pidx0 = take(cap * 4u);
@@ -86,12 +104,11 @@ PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap 
     L.rng = take(cap * 8u);
     L.light_aux = take((uint64_t)(n_lights ? n_lights : 1) * 16u);
     L.light_cdf = take((uint64_t)(n_lights ? n_lights : 1) * 4u + 16u);
-    L.counters = take(kCntWords * 4u);
     L.stage = take(cap * 32u);
     L.stage_pidx = take(cap * 4u);
     L.stage_rank = take(cap * 4u);
     L.train_cap = train_cap;
-    const uint64_t qcap = train_cap ? cap : 0;
+    const uint64_t qcap = train_cap ? npix : 0;
     L.qin = take(qcap * 48u);
     L.qout = take(qcap * 16u);
     L.qt1 = take(qcap * 16u);
@@ -190,6 +207,7 @@ struct PtArgs {
     // batch (multi-scene kernels): each queue entry carries its scene
     const BtScene *bt;
     uint32_t wave_base;        // global path index of slot 0 of the wave
+    uint32_t npix;             // single scene: pixels (path q of a wave is pixel q % npix)
     const uint32_t *rsid_in;
     uint32_t *rsid_out;
     uint32_t *ssid;
@@ -226,27 +244,29 @@ __global__ void k_pt_setup(const rt_pt_light *lights, uint32_t n_lights, float4 
 
 __global__ void __launch_bounds__(kPtThreads) k_pt_raygen(float ax, float ay, float cx, float cy, float cz,
                                                            uint32_t w, uint32_t h, uint64_t seed,
-                                                           const uint32_t *sample_dev, float4 *rays, uint32_t *pidx,
-                                                           float4 *tput, float4 *rad, uint64_t *rng,
+                                                           const uint32_t *sample_dev, uint32_t k, float4 *rays,
+                                                           uint32_t *pidx, float4 *tput, float4 *rad, uint64_t *rng,
                                                            uint32_t *count0, unsigned long long *ray_counts) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    // path q of the wave: sample (*sample_dev + q / n) of pixel q % n
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = w * h;
-    if (p == 0) {
-        *count0 = n;
-        atomicAdd(ray_counts, (unsigned long long)n);
+    if (q == 0) {
+        *count0 = n * k;
+        atomicAdd(ray_counts, (unsigned long long)n * k);
     }
-    if (p >= n) return;
+    if (q >= n * k) return;
+    const uint32_t j = q / n, p = q - j * n;
     const uint32_t x = p % w, y = p / w;
-    rtpt::Pcg g = rtpt::pcg_seed(seed, *sample_dev, p);
+    rtpt::Pcg g = rtpt::pcg_seed(seed, *sample_dev + j, p);
     const float jx = rtpt::pcg_uniform(g), jy = rtpt::pcg_uniform(g);
     float d[3];
     rtpt::camera_dir(ax, ay, w, h, x, y, jx, jy, d);
-    rays[2u * p] = make_float4(cx, cy, cz, 0.0f);
-    rays[2u * p + 1u] = make_float4(d[0], d[1], d[2], 1e30f);
-    pidx[p] = p;
-    tput[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    rad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    rng[p] = g.state;
+    rays[2u * q] = make_float4(cx, cy, cz, 0.0f);
+    rays[2u * q + 1u] = make_float4(d[0], d[1], d[2], 1e30f);
+    pidx[q] = q;
+    tput[q] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    rad[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    rng[q] = g.state;
 }
 
 // One slot per voting lane of the warp in the queue behind `count`.
@@ -322,7 +342,7 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
         const float4 *light_aux = a.light_aux;
         const float *light_cdf = a.light_cdf;
         uint32_t n_lights = a.n_lights;
-        uint32_t pix = p;  // pixel index within the scene: the random stream
+        uint32_t pix = (!MULTI && a.npix) ? p % a.npix : p;  // pixel index within the scene: the random stream
         if (MULTI) {
             sid = a.rsid_in[i];
             const BtScene &sc = a.bt[sid];
@@ -573,17 +593,21 @@ __global__ void __launch_bounds__(512) k_pt_resolve(const uint32_t *scount, cons
     }
 }
 
-__global__ void __launch_bounds__(kPtThreads) k_pt_accumulate(uint32_t n, const float4 *rad, float4 *accum,
-                                                               uint32_t *sample_dev) {
+// Adds the wave's k samples of pixel p in sample order (the order
+// consecutive one-sample waves would add them).
+__global__ void __launch_bounds__(kPtThreads) k_pt_accumulate(uint32_t n, uint32_t k, const float4 *rad,
+                                                               float4 *accum, uint32_t *sample_dev) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p == 0) *sample_dev = *sample_dev + 1u;  // raygen of this sample already read it
+    if (p == 0) *sample_dev = *sample_dev + k;  // raygen of this wave already read it
     if (p >= n) return;
-    const float4 r = rad[p];
     float4 acc = accum[p];
-    acc.x = acc.x + r.x;
-    acc.y = acc.y + r.y;
-    acc.z = acc.z + r.z;
-    acc.w = acc.w + 1.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        const float4 r = rad[(size_t)j * n + p];
+        acc.x = acc.x + r.x;
+        acc.y = acc.y + r.y;
+        acc.z = acc.z + r.z;
+        acc.w = acc.w + 1.0f;
+    }
     accum[p] = acc;
 }
 
@@ -773,6 +797,7 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
     a.eps = p->ray_eps;
     a.ray_counts = ray_counts;
     a.err = ctx->d_err;
+    a.npix = (uint32_t)npix;
     if (cp) {
         a.cache_mode = 1;
         a.stride = train_stride(npix, cp->train_paths);
@@ -791,25 +816,28 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
     float4 *rays[2] = {reinterpret_cast<float4 *>(S + L.rays0), reinterpret_cast<float4 *>(S + L.rays1)};
     uint32_t *pidx[2] = {reinterpret_cast<uint32_t *>(S + L.pidx0), reinterpret_cast<uint32_t *>(S + L.pidx1)};
     uint8_t *socc = S + L.socc;
+    const uint64_t cap = L.cap;  // paths of a full wave: pixels x L.wave samples
     const unsigned blocks = (unsigned)((npix + kPtThreads - 1) / kPtThreads);
-    const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<false>, kPtThreads, npix);
-    const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, kPtThreads, npix);
-    const unsigned scatter_blocks = resident_blocks(ctx, (const void *)k_pt_bin_scatter<false>, kPtThreads, npix);
+    const unsigned shade_blocks = resident_blocks(ctx, (const void *)k_pt_shade<false>, kPtThreads, cap);
+    const unsigned resolve_blocks = resident_blocks(ctx, (const void *)k_pt_resolve, kPtThreads, cap);
+    const unsigned scatter_blocks = resident_blocks(ctx, (const void *)k_pt_bin_scatter<false>, kPtThreads, cap);
     a.binning = (p->flags & RT_PT_OCTANT_BINNING) ? 1u : 0u;
     a.stage = reinterpret_cast<float4 *>(S + L.stage);
     a.stage_pidx = reinterpret_cast<uint32_t *>(S + L.stage_pidx);
     a.stage_rank = reinterpret_cast<uint32_t *>(S + L.stage_rank);
 
-    for (uint32_t s = 0; s < p->spp; ++s) {
+    for (uint32_t s = 0, kw = 0; s < p->spp; s += kw) {
+        // one wave: kw samples of every pixel (kw = L.wave but for the last)
+        kw = p->spp - s < L.wave ? p->spp - s : L.wave;
+        const uint32_t nw = (uint32_t)(npix * kw);  // paths of this wave
         RT_CUDA_CTX(ctx, cudaMemsetAsync(cnt, 0, kCntPerSample * 4u, st));
-        k_pt_raygen<<<blocks, kPtThreads, 0, st>>>(ax, ay, p->camera.position[0], p->camera.position[1],
-                                                   p->camera.position[2], p->width, p->height, p->seed, sample_dev,
-                                                   rays[0], pidx[0], a.tput, a.rad, a.rng, &cnt[0], ray_counts);
+        k_pt_raygen<<<(unsigned)((nw + kPtThreads - 1u) / kPtThreads), kPtThreads, 0, st>>>(
+            ax, ay, p->camera.position[0], p->camera.position[1], p->camera.position[2], p->width, p->height,
+            p->seed, sample_dev, kw, rays[0], pidx[0], a.tput, a.rad, a.rng, &cnt[0], ray_counts);
         RT_CUDA_CTX(ctx, cudaGetLastError());
         // depth 0's extension rays alone; afterwards each launch traces a
         // depth's shadow rays together with the next depth's extension rays
-        int rc0 = launch_queue_trace(ctx, st, accel, rays[0], S + L.hits, nullptr, &cnt[0], (uint32_t)npix, &tcnt[0],
-                                     false);
+        int rc0 = launch_queue_trace(ctx, st, accel, rays[0], S + L.hits, nullptr, &cnt[0], nw, &tcnt[0], false);
         if (rc0) return rc0;
         for (uint32_t d = 0; d < p->max_depth; ++d) {
             const uint32_t q = d & 1u;
@@ -828,12 +856,12 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
             if (a.binning && d + 1u < p->max_depth) {
                 k_pt_bin_scatter<false><<<scatter_blocks, kPtThreads, 0, st>>>(
                     &cnt[d + 1], a.bins_out, a.stage, a.stage_pidx, nullptr, a.stage_rank, rays[q ^ 1u],
-                    pidx[q ^ 1u], nullptr, (uint32_t)npix, ctx->d_err);
+                    pidx[q ^ 1u], nullptr, nw, ctx->d_err);
                 RT_CUDA_CTX(ctx, cudaGetLastError());
             }
             // cnt[max_depth] stays 0: the last launch traces shadow rays only
             rc = launch_queue_trace_mixed(ctx, st, accel, rays[q ^ 1u], S + L.hits, &cnt[d + 1], a.srays, socc,
-                                          &scnt[d], (uint32_t)npix, &tcnt[2 * d + 1]);
+                                          &scnt[d], nw, &tcnt[2 * d + 1]);
             if (rc) return rc;
             k_pt_resolve<<<resolve_blocks, kPtThreads, 0, st>>>(&scnt[d], socc, a.spidx, a.scontrib, a.rad);
             RT_CUDA_CTX(ctx, cudaGetLastError());
@@ -848,7 +876,7 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
                                                             a.tcount, a.tpidx, a.tt1, a.tlpre, ttarget);
             RT_CUDA_CTX(ctx, cudaGetLastError());
         }
-        k_pt_accumulate<<<blocks, kPtThreads, 0, st>>>((uint32_t)npix, a.rad, reinterpret_cast<float4 *>(accum),
+        k_pt_accumulate<<<blocks, kPtThreads, 0, st>>>((uint32_t)npix, kw, a.rad, reinterpret_cast<float4 *>(accum),
                                                        sample_dev);
         RT_CUDA_CTX(ctx, cudaGetLastError());
         if (cp && cp->train_batch) {
