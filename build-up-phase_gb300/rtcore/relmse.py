@@ -4,9 +4,12 @@ path tracer, both measured against a converged plain reference.
     python -m rtcore.relmse [--spheres 160 --freq 50] [--width 1920 --height 1080]
                             [--ref-spp 16384] [--budget-ms 4000] [--out result.json]
 
-relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Both
-forms run one sample per call; the time of a call is its CUDA-event duration
-(training included for the learned form), image read-backs are not timed.
+relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Each
+form runs in its fastest mode: the plain path tracer four samples per call
+(one wave of four samples of every pixel), the learned form one sample per
+call (its waves hold one sample; training follows each); the time of a call
+is its CUDA-event duration (training included for the learned form), image
+read-backs are not timed.
 The curve is sampled at sample counts growing by 1.25x and at the end of the
 budget; the time to a target relMSE is interpolated log-log between the two
 samples around the crossing.
@@ -86,12 +89,14 @@ def _checkpoints(n: int):
 
 
 def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, cached: bool,
-        train_paths: int = 65536, train_batch: int = 16384, seed: int = 777, lr: float = 1e-3):
+        train_paths: int = 65536, train_batch: int = 16384, seed: int = 777, lr: float = 1e-3,
+        spp_per_call: int = 1):
     """[(elapsed_ms, samples, relmse)] within the time budget."""
     import torch
     st = torch.cuda.current_stream()
     accum = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
-    p = params(w, h, 1, 0, seed)
+    spc = max(1, spp_per_call)
+    p = params(w, h, spc, 0, seed)
     cache = None
     if cached:
         cache = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device="cuda")
@@ -105,7 +110,7 @@ def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: f
     marks = set(_checkpoints(1 << 20))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     while elapsed < budget_ms:
-        p = params(w, h, 1, s, seed)
+        p = params(w, h, spc, s, seed)
         e0.record(st)
         if cached:
             ctx.path_trace_cached(box.scene, p, cp, accum, scratch, nb)
@@ -114,8 +119,8 @@ def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: f
         e1.record(st)
         e1.synchronize()
         elapsed += e0.elapsed_time(e1)
-        s += 1
-        if s in marks or elapsed >= budget_ms:
+        s += spc
+        if any(k in marks for k in range(s - spc + 1, s + 1)) or elapsed >= budget_ms:
             curve.append((round(elapsed, 3), s, relmse(_image(accum), ref)))
     ctx.sync()
     return curve
@@ -149,6 +154,8 @@ def main(argv=None) -> int:
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--train-paths", type=int, default=65536, help="training paths per frame")
     ap.add_argument("--train-batch", type=int, default=16384)
+    ap.add_argument("--plain-spp-per-call", type=int, default=4,
+                    help="samples per call of the plain form (4: one wave of four samples)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     load()
@@ -157,11 +164,12 @@ def main(argv=None) -> int:
     box = GpuBox(ctx, a.spheres, a.freq)
     ref = reference(ctx, box, a.width, a.height, a.ref_spp)
     t_ref = time.time() - t0
-    plain = run(ctx, box, a.width, a.height, ref, a.budget_ms, False)
+    plain = run(ctx, box, a.width, a.height, ref, a.budget_ms, False, spp_per_call=a.plain_spp_per_call)
     cached = run(ctx, box, a.width, a.height, ref, a.budget_ms, True, train_paths=a.train_paths,
                  train_batch=a.train_batch, lr=a.lr)
     res = {"tris": box.n_tris, "width": a.width, "height": a.height, "ref_spp": a.ref_spp,
            "train_paths": a.train_paths, "train_batch": a.train_batch, "lr": a.lr,
+           "plain_spp_per_call": a.plain_spp_per_call, "cached_spp_per_call": 1,
            "reference_wall_s": round(t_ref, 1), "budget_ms": a.budget_ms,
            "plain": plain, "cached": cached,
            "relmse_at_budget": {"plain": plain[-1][2], "cached": cached[-1][2]},
