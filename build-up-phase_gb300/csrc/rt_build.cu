@@ -349,12 +349,16 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ boxes,
     float lo[3], scale[3];
     const float maxq = (float)((1u << bpa) - 1u), cells = (float)(1u << bpa);
     const bool any = cbounds[0] != INT32_MAX;
+    float cext = 0.0f;  // longest axis of the centroid bounds
     for (int a = 0; a < 3; ++a) {
         float l = any ? ford_inv(cbounds[a]) : 0.0f, h = any ? ford_inv(cbounds[3 + a]) : 0.0f;
         float ext = h - l;
         lo[a] = l;
         scale[a] = ext > 0.0f ? cells / ext : 0.0f;
+        if (ext > cext) cext = ext;
     }
+    const float large = RT_LARGE_PRIM_FRACTION * cext;
+    const uint64_t large_bit = bpa == 21 ? (1ull << 63) : (1ull << 31);
     const uint64_t inactive = bpa == 21 ? ((1ull << 63) - 1ull) : ((1ull << 30) - 1ull);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         Box b = load_box(boxes, i);
@@ -369,6 +373,12 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ boxes,
                 q[a] = !(f > 0.0f) ? 0u : (f >= maxq ? (uint32_t)maxq : (uint32_t)f);
             }
             key = spread3_21(q[0]) | (spread3_21(q[1]) << 1) | (spread3_21(q[2]) << 2);
+            float e = 0.0f;  // longest axis of the primitive's box
+            for (int a = 0; a < 3; ++a) {
+                const float x = b.hi[a] - b.lo[a];
+                if (x > e) e = x;
+            }
+            if (e > large) key |= large_bit;
         }
         keys[i] = key;
         ids[i] = i;

@@ -39,6 +39,14 @@
 #define RT_SAH_PRIM 1.0f
 #define RT_SAH_NODE 0.3f
 
+/* A primitive whose box is longer, on its longest axis, than this fraction of
+ * the longest axis of the centroid bounds is "large": its sort key gets the
+ * bit above the Morton code (bit 63 of the 63-bit keys, bit 31 of the 30-bit
+ * ones), so the radix tree's root separates the large primitives from the
+ * rest and the small primitives' node boxes are not stretched by them (the
+ * walls of a room around small objects).  0.25 is exact in binary. */
+#define RT_LARGE_PRIM_FRACTION 0.25f
+
 /* Smallest / largest per-axis exponent of a node's quantisation grid. */
 #define RT_QEXP_MIN (-100)
 #define RT_QEXP_MAX (100)

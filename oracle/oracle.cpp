@@ -284,6 +284,25 @@ Tree build_tree(const BuildInput &in, uint32_t flags, uint32_t &morton_bits, orc
     std::vector<uint64_t> keys(n);
     for (uint32_t i = 0; i < n; ++i)
         keys[i] = in.active[i] ? morton_key(g, &cent[(size_t)i * 3]) : inactive_key;
+    /* large primitives (RT_LARGE_PRIM_FRACTION): the bit above the Morton code */
+    {
+        float cext = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            float x = ford_inv(chi[a]) - ford_inv(clo[a]);
+            if (x > cext) cext = x;
+        }
+        const float large = RT_LARGE_PRIM_FRACTION * cext;
+        const uint64_t large_bit = (bpa == 21) ? (1ull << 63) : (1ull << 31);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (!in.active[i]) continue;
+            float e = 0.0f;
+            for (int a = 0; a < 3; ++a) {
+                float x = in.boxes[i].hi[a] - in.boxes[i].lo[a];
+                if (x > e) e = x;
+            }
+            if (e > large) keys[i] |= large_bit;
+        }
+    }
     if (dbg && dbg->keys_unsorted) std::memcpy(dbg->keys_unsorted, keys.data(), n * 8ull);
 
     /* stable sort by key (what an LSD radix sort produces) */
