@@ -59,7 +59,7 @@ typedef struct rt_pt_params {
  * child visiting order.  The images do not depend on the order.  Off by
  * default: on the GB300 the rays' spatial order (pixel order) is worth more
  * to the traversal than their directional order -- 2M-triangle box at
- * 1920x1080, 4 spp per call: 7.59 ms per sample in shading order, 7.85 ms
+ * 1920x1080, 4 spp per call: 6.72 ms per sample in shading order, 7.01 ms
  * binned. */
 #define RT_PT_OCTANT_BINNING 1u
 
