@@ -104,6 +104,33 @@ def test_blas_extreme_coordinates_bit_exact(ctx, orc, seed, frac):
     compare_accels(g.bytes(), o, 48)
 
 
+@pytest.mark.parametrize("kind,flags", [("box", M30), ("all_large", 0), ("half_large", 0), ("half_large", M30)])
+def test_blas_large_primitives_bit_exact(ctx, orc, kind, flags):
+    """Primitives longer than RT_LARGE_PRIM_FRACTION of the centroid bounds
+    take the key bit above the Morton code (bit 63, or bit 31 with 30-bit
+    keys): a room's walls among small objects, a scene of large triangles
+    only, and an even mix -- bit-exact with the oracle."""
+    import rtcore.scenes as S
+    rng = np.random.default_rng(17)
+    if kind == "box":
+        v, i, _, _ = S.box(S.SEED_BASE + 3, 3, 6)
+    else:
+        n_big = 400 if kind == "all_large" else 200
+        c = rng.uniform(0, 1, size=(n_big, 1, 3)).astype(np.float32)
+        big = (c + rng.uniform(-0.6, 0.6, size=(n_big, 3, 3))).astype(np.float32).reshape(-1, 3)
+        parts = [big]
+        if kind == "half_large":
+            c2 = rng.uniform(0, 1, size=(200, 1, 3)).astype(np.float32)
+            parts.append((c2 + rng.uniform(-0.01, 0.01, size=(200, 3, 3))).astype(np.float32).reshape(-1, 3))
+        v = np.concatenate(parts)
+        i = np.arange(len(v), dtype=np.uint32).reshape(-1, 3)
+    items = [(v, i, None)]
+    g = GpuBlas(ctx, items, flags)
+    o, rc = orc.build_blas(items, flags)
+    assert rc == 0
+    compare_accels(g.bytes(), o, 48)
+
+
 def test_blas_box_scene_bit_exact(ctx, orc):
     import rtcore.scenes as S
     v, i, tm, m = S.box(S.SEED_BASE + 3, 6, 12)
