@@ -82,7 +82,7 @@ extern "C" rt_status rt_context_create(int device, rt_context **out) {
         return RT_ERR_CUDA;
     }
     ctx->tuning.block_threads = 128;
-    ctx->tuning.blocks_per_sm = 8;
+    ctx->tuning.blocks_per_sm = 9;
     // refill a warp once 4 lanes are idle: best for incoherent rays in a
     // sweep of 1..32 on the 1M-triangle soup (primary rays are flat from 4
     // to 16)

@@ -84,8 +84,12 @@ struct BatchArgs {
 // occluded) -- each ray walked exactly as in a launch of its own kind; the
 // path tracer traces a depth's shadow rays and the next depth's extension
 // rays together, so the two share one launch tail.
+// Register budget: the single-structure kernels fit nine 128-thread blocks
+// per SM (56 registers, no spill; 36 warps against 32 at 64 registers:
+// 2,093 -> 2,111 M rays/s on the 1M soup, 6.72 -> 6.58 ms per path-traced
+// sample); the multi-scene ones keep eight (they spill at 56).
 template <bool ANY, bool STATS, bool MULTI, int THREADS, int RING, bool MIXED = false>
-__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_trace_blas(const BatchArgs a) {
+__global__ void __launch_bounds__(THREADS, (MULTI ? 1024 : 1152) / THREADS) k_trace_blas(const BatchArgs a) {
     static_assert((RING & (RING - 1)) == 0 && RING <= kMaxDepth, "RING is a power of two");
     __shared__ uint2 s_stack[RING][THREADS];
     const uint4 *nodes = nullptr, *prims = nullptr;
