@@ -44,7 +44,7 @@ def _scene(rng):
     return v.astype(np.float32), i, scale
 
 
-@pytest.mark.parametrize("seed", range(12))
+@pytest.mark.parametrize("seed", range(32))
 def test_random_scene_build_and_trace(ctx, orc, seed):
     import rtcore
     import rtcore.scenes as S
