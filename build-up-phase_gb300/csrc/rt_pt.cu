@@ -51,15 +51,14 @@ struct PtLayout {
     uint32_t wave;  // samples of every pixel traced together (cap = pixels x wave)
 };
 
-// Samples per pixel traced as one wave by the plain path tracer: a wave of
-// k samples has k times the rays per traversal launch, so each launch's
-// slow-ray tail is shared by k samples.  At most 4, and at most 2^23 paths
-// (~1.9 GB of path state and queues); the learned form keeps one sample per
-// wave (its training pixels are chosen per sample).
+// Samples per pixel traced as one wave: a wave of k samples has k times the
+// rays per traversal launch, so each launch's slow-ray tail is shared by k
+// samples.  At most 4, and at most 2^23 paths (~1.9 GB of path state and
+// queues).  The learned form queries the cache once per wave and trains on
+// the wave's training paths after it.
 constexpr uint32_t kPtWaveSamples = 4;
 constexpr uint64_t kPtWavePaths = 1ull << 23;
-inline uint32_t wave_samples(uint64_t npix, uint32_t spp, bool cached) {
-    if (cached) return 1u;
+inline uint32_t wave_samples(uint64_t npix, uint32_t spp) {
     uint64_t k = spp < kPtWaveSamples ? spp : kPtWaveSamples;
     while (k > 1u && npix * k > kPtWavePaths) --k;
     return (uint32_t)(k ? k : 1u);
@@ -80,7 +79,7 @@ constexpr uint32_t kCntWords = 800;
 PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap = 0) {
     PtLayout L;
     const uint64_t npix = (uint64_t)p.width * p.height;
-    L.wave = wave_samples(npix, p.spp, train_cap > 0);
+    L.wave = wave_samples(npix, p.spp);
     const uint64_t cap = npix * L.wave;
     L.cap = (uint32_t)cap;
     uint64_t off = 0;
@@ -107,17 +106,18 @@ PtLayout pt_layout(const rt_pt_params &p, uint32_t n_lights, uint32_t train_cap 
     L.stage = take(cap * 32u);
     L.stage_pidx = take(cap * 4u);
     L.stage_rank = take(cap * 4u);
-    L.train_cap = train_cap;
-    const uint64_t qcap = train_cap ? npix : 0;
+    // train_cap: training paths of one sample; a wave holds L.wave samples'
+    L.train_cap = train_cap * L.wave;
+    const uint64_t qcap = train_cap ? cap : 0;
     L.qin = take(qcap * 48u);
     L.qout = take(qcap * 16u);
     L.qt1 = take(qcap * 16u);
     L.qpidx = take(qcap * 4u);
-    L.tin = take((uint64_t)train_cap * 48u);
-    L.ttarget = take((uint64_t)train_cap * 16u);
-    L.tt1 = take((uint64_t)train_cap * 16u);
-    L.tlpre = take((uint64_t)train_cap * 16u);
-    L.tpidx = take((uint64_t)train_cap * 4u);
+    L.tin = take((uint64_t)L.train_cap * 48u);
+    L.ttarget = take((uint64_t)L.train_cap * 16u);
+    L.tt1 = take((uint64_t)L.train_cap * 16u);
+    L.tlpre = take((uint64_t)L.train_cap * 16u);
+    L.tpidx = take((uint64_t)L.train_cap * 4u);
     L.total = off;
     return L;
 }
@@ -407,8 +407,10 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
                     // second vertex of the learned form: record (x, -d, n,
                     // albedo); training pixels go on as plain path tracing,
                     // the others end here in a cache query
-                    const uint32_t off =
-                        (uint32_t)(rtpt::splitmix64(a.seed ^ (0x5851f42d4c957f2dull + *a.sample_dev)) % a.stride);
+                    // path p of the wave: sample (*sample_dev + p / npix) of pixel p % npix
+                    const uint32_t jw = p / a.npix, pixp = p - jw * a.npix;
+                    const uint32_t off = (uint32_t)(
+                        rtpt::splitmix64(a.seed ^ (0x5851f42d4c957f2dull + *a.sample_dev + jw)) % a.stride);
                     for (int k = 0; k < 3; ++k) {
                         crec.pos[k] = P[k];
                         crec.dir[k] = -d[k];
@@ -416,7 +418,7 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
                         crec.albedo[k] = m.albedo[k];
                     }
                     t1 = T;
-                    if ((p + off) % a.stride == 0u) {
+                    if ((pixp + off) % a.stride == 0u) {
                         is_train = true;
                         lpre = a.rad[p];
                     } else {
@@ -868,12 +870,11 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
         }
         float4 *ttarget = reinterpret_cast<float4 *>(S + L.ttarget);
         if (cp) {
-            int rc = cache_query_dev(ctx, st, cp->cache, a.qin, reinterpret_cast<float *>(S + L.qout), a.qcount,
-                                     (uint32_t)npix);
+            int rc = cache_query_dev(ctx, st, cp->cache, a.qin, reinterpret_cast<float *>(S + L.qout), a.qcount, nw);
             if (rc) return rc;
-            k_pt_cache_apply<<<blocks, kPtThreads, 0, st>>>(a.qcount, a.qpidx, a.qt1,
-                                                            reinterpret_cast<const float4 *>(S + L.qout), a.rad,
-                                                            a.tcount, a.tpidx, a.tt1, a.tlpre, ttarget);
+            k_pt_cache_apply<<<(unsigned)((nw + kPtThreads - 1u) / kPtThreads), kPtThreads, 0, st>>>(
+                a.qcount, a.qpidx, a.qt1, reinterpret_cast<const float4 *>(S + L.qout), a.rad, a.tcount, a.tpidx,
+                a.tt1, a.tlpre, ttarget);
             RT_CUDA_CTX(ctx, cudaGetLastError());
         }
         k_pt_accumulate<<<blocks, kPtThreads, 0, st>>>((uint32_t)npix, kw, a.rad, reinterpret_cast<float4 *>(accum),
@@ -881,7 +882,7 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
         RT_CUDA_CTX(ctx, cudaGetLastError());
         if (cp && cp->train_batch) {
             int rc = cache_train_dev(ctx, st, cp->cache, a.tin, reinterpret_cast<const float *>(ttarget), a.tcount,
-                                     tcap, cp->train_batch);
+                                     tcap * kw, cp->train_batch);
             if (rc) return rc;
         }
     }

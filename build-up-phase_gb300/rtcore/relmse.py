@@ -4,12 +4,11 @@ path tracer, both measured against a converged plain reference.
     python -m rtcore.relmse [--spheres 160 --freq 50] [--width 1920 --height 1080]
                             [--ref-spp 16384] [--budget-ms 4000] [--out result.json]
 
-relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Each
-form runs in its fastest mode: the plain path tracer four samples per call
-(one wave of four samples of every pixel), the learned form one sample per
-call (its waves hold one sample; training follows each); the time of a call
-is its CUDA-event duration (training included for the learned form), image
-read-backs are not timed.
+relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Both
+forms run four samples per call (one wave of four samples of every pixel; the
+learned form queries the cache once per wave and trains after it on the
+wave's training paths); the time of a call is its CUDA-event duration
+(training included for the learned form), image read-backs are not timed.
 The curve is sampled at sample counts growing by 1.25x and at the end of the
 budget; the time to a target relMSE is interpolated log-log between the two
 samples around the crossing.
@@ -156,6 +155,8 @@ def main(argv=None) -> int:
     ap.add_argument("--train-batch", type=int, default=16384)
     ap.add_argument("--plain-spp-per-call", type=int, default=4,
                     help="samples per call of the plain form (4: one wave of four samples)")
+    ap.add_argument("--cached-spp-per-call", type=int, default=4,
+                    help="samples per call of the learned form (the cache trains after each call's wave)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     load()
@@ -166,10 +167,10 @@ def main(argv=None) -> int:
     t_ref = time.time() - t0
     plain = run(ctx, box, a.width, a.height, ref, a.budget_ms, False, spp_per_call=a.plain_spp_per_call)
     cached = run(ctx, box, a.width, a.height, ref, a.budget_ms, True, train_paths=a.train_paths,
-                 train_batch=a.train_batch, lr=a.lr)
+                 train_batch=a.train_batch, lr=a.lr, spp_per_call=a.cached_spp_per_call)
     res = {"tris": box.n_tris, "width": a.width, "height": a.height, "ref_spp": a.ref_spp,
            "train_paths": a.train_paths, "train_batch": a.train_batch, "lr": a.lr,
-           "plain_spp_per_call": a.plain_spp_per_call, "cached_spp_per_call": 1,
+           "plain_spp_per_call": a.plain_spp_per_call, "cached_spp_per_call": a.cached_spp_per_call,
            "reference_wall_s": round(t_ref, 1), "budget_ms": a.budget_ms,
            "plain": plain, "cached": cached,
            "relmse_at_budget": {"plain": plain[-1][2], "cached": cached[-1][2]},

@@ -86,8 +86,11 @@ rt_status rt_path_trace(rt_context *ctx, rt_stream stream, const rt_pt_scene *sc
  * through the second vertex (divided by the throughput there) is a training
  * target for (position, direction toward the first vertex, normal, albedo).
  * Every other path adds throughput x max(cache, 0) at its second vertex and
- * stops.  After the wave the cache takes ceil(train_paths / train_batch) Adam
- * steps on the new samples (train_batch 0: no training).  The cache's
+ * stops.  A wave holds up to four of the call's samples (see
+ * rt_pt_scratch_bytes): its paths query the cache as it stood before the
+ * wave, and after the wave the cache takes ceil(training paths / train_batch)
+ * Adam steps on the wave's training paths (train_batch 0: no training), so a
+ * call of one sample trains after every sample.  The cache's
  * emission is not included: direct light reaches the first vertex through
  * next-event estimation only, as in the plain form.
  */

@@ -22,34 +22,39 @@ def box(ctx):
     return GpuBox(ctx, 40, 50)
 
 
-def _frames(ctx, box, w, h, frames, train_batch, train_paths, seed=11):
+def _frames(ctx, box, w, h, frames, train_batch, train_paths, seed=11, spc=1):
+    """frames training samples then 32 measured ones, spc samples per call
+    (one wave of spc samples: the cache trains after each call)."""
     import torch
     import rtcore
     from rtcore.relmse import _image, params
     cache = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device="cuda")
     ctx.cache_init(cache, rtcore.cache_config(seed=5))
     cp = rtcore.PtCacheParams(cache.data_ptr(), train_paths, train_batch)
-    p = params(w, h, 1, 0, seed)
+    p = params(w, h, spc, 0, seed)
     nb = ctx.pt_cached_scratch_bytes(p, cp)
     scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
     warm = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
-    for s in range(frames):  # training frames (their image is discarded)
-        ctx.path_trace_cached(box.scene, params(w, h, 1, s, seed), cp, warm, scratch, nb)
+    for s in range(0, frames, spc):  # training frames (their image is discarded)
+        ctx.path_trace_cached(box.scene, params(w, h, spc, s, seed), cp, warm, scratch, nb)
     accum = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
-    for s in range(frames, frames + 32):
-        ctx.path_trace_cached(box.scene, params(w, h, 1, s, seed), cp, accum, scratch, nb)
+    for s in range(frames, frames + 32, spc):
+        ctx.path_trace_cached(box.scene, params(w, h, spc, s, seed), cp, accum, scratch, nb)
     ctx.sync()
     img = _image(accum)
     assert np.isfinite(img).all() and (img >= 0).all()
     return img
 
 
-def test_training_gains_over_untrained_cache(ctx, box):
+@pytest.mark.parametrize("spc", [1, 4])
+def test_training_gains_over_untrained_cache(ctx, box, spc):
+    """One sample per call (training after every sample) and four (one wave
+    of four samples per call, training after the wave)."""
     from rtcore.relmse import reference, relmse
     w, h = 480, 270
     ref = reference(ctx, box, w, h, 1024)
-    trained = _frames(ctx, box, w, h, 64, 4096, 4096)
-    untrained = _frames(ctx, box, w, h, 64, 0, 4096)
+    trained = _frames(ctx, box, w, h, 64, 4096, 4096, spc=spc)
+    untrained = _frames(ctx, box, w, h, 64, 0, 4096, spc=spc)
     r_t, r_u = relmse(trained, ref), relmse(untrained, ref)
     assert r_t < 0.5 * r_u, (r_t, r_u)
 
