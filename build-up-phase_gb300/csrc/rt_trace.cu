@@ -364,6 +364,7 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     a.counter = acquire_counter(ctx, st);
     if (!a.counter) return set_error(ctx, RT_ERR_CUDA, "work counter reset failed");
     uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
+    if (any && per_sm > kAnyBlocksPerSm) per_sm = kAnyBlocksPerSm;
     uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
     uint32_t need = (n + kTraceThreads - 1) / kTraceThreads;
     if (blocks > need) blocks = need;
@@ -416,6 +417,7 @@ int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, c
     a.out_rec = 1;
     a.counter = counter;
     uint32_t per_sm = ctx->tuning.blocks_per_sm ? ctx->tuning.blocks_per_sm : 8u;
+    if (any && per_sm > kAnyBlocksPerSm) per_sm = kAnyBlocksPerSm;
     uint32_t blocks = per_sm * (uint32_t)ctx->sm_count;
     uint32_t need = (max_n + kTraceThreads - 1) / kTraceThreads;
     if (blocks > need) blocks = need;

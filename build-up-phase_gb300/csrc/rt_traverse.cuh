@@ -30,6 +30,7 @@ namespace {
 
 constexpr int kTraceThreads = 128;  // block size of the single-structure kernels
 constexpr int kRing = 16;           // shared-memory stack entries per ray (single-structure kernels)
+constexpr uint32_t kAnyBlocksPerSm = 1024u / kTraceThreads;  // resident blocks the any-hit kernel is bounded for
 constexpr int kMaxDepth = 64;       // total stack entries per ray
 constexpr uint32_t kNone = 0xffffffffu;
 
@@ -84,12 +85,14 @@ struct BatchArgs {
 // occluded) -- each ray walked exactly as in a launch of its own kind; the
 // path tracer traces a depth's shadow rays and the next depth's extension
 // rays together, so the two share one launch tail.
-// Register budget: the single-structure kernels fit nine 128-thread blocks
-// per SM (56 registers, no spill; 36 warps against 32 at 64 registers:
-// 2,093 -> 2,111 M rays/s on the 1M soup, 6.72 -> 6.58 ms per path-traced
-// sample); the multi-scene ones keep eight (they spill at 56).
+// Register budget: the closest-hit and mixed single-structure kernels fit
+// nine 128-thread blocks per SM (56 registers, no spill; 36 warps against 32
+// at 64 registers: 2,093 -> 2,111 M rays/s on the 1M soup, 6.72 -> 6.58 ms
+// per path-traced sample).  The any-hit and multi-scene kernels keep eight
+// blocks and 64 registers: any-hit shadow rays run 1,287 M rays/s there
+// against 1,202 at nine blocks, and the multi-scene kernels spill at 56.
 template <bool ANY, bool STATS, bool MULTI, int THREADS, int RING, bool MIXED = false>
-__global__ void __launch_bounds__(THREADS, (MULTI ? 1024 : 1152) / THREADS) k_trace_blas(const BatchArgs a) {
+__global__ void __launch_bounds__(THREADS, ((MULTI || ANY) ? 1024 : 1152) / THREADS) k_trace_blas(const BatchArgs a) {
     static_assert((RING & (RING - 1)) == 0 && RING <= kMaxDepth, "RING is a power of two");
     __shared__ uint2 s_stack[RING][THREADS];
     const uint4 *nodes = nullptr, *prims = nullptr;
