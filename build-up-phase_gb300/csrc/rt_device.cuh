@@ -194,6 +194,37 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return d;
 }
 
+// Two-wide FP32 arithmetic (PTX .f32x2, sm_100 and later): one instruction
+// for two lanes' worth of add or fma, each half rounded exactly as the scalar
+// instruction, so the pair equals two scalar results bit for bit.
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// Byte b of wx and of wy as the pair (2^23 + qx, 2^23 + qy); adding
+// (-2^23, -2^23) leaves the exact byte values.
+__device__ __forceinline__ uint64_t qpair2_biased(uint32_t wx, uint32_t wy, int b) {
+    const uint32_t lo = __byte_perm(wx, 0x4B000000u, 0x7540u | (uint32_t)b);
+    const uint32_t hi = __byte_perm(wy, 0x4B000000u, 0x7540u | (uint32_t)b);
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(lo), "r"(hi));
+    return d;
+}
+
 // Box test of a node's 8 children against [tmin, tcur].
 //   node_hits: bit (slot ^ oct) for every internal child hit
 //   prim_hits: leaf-record mask relative to the node's prim_base
@@ -201,6 +232,7 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
 // below 24, so XOR-ing the octant into the internal bytes (four at a time)
 // lets one shift-or per hit slot build both masks: internal children land on
 // bit 24 + (slot ^ oct), leaf records on their offsets.
+template <bool PAIR_Z = false>
 __device__ __forceinline__ void isect_node(const Ray &r, const NodeWords &n, float tmin, float tcur,
                                            uint32_t &node_hits, uint32_t &prim_hits) {
     const float px = __uint_as_float(n.w0.x), py = __uint_as_float(n.w0.y), pz = __uint_as_float(n.w0.z);
@@ -216,6 +248,11 @@ __device__ __forceinline__ void isect_node(const Ray &r, const NodeWords &n, flo
     const uint32_t hix[2] = {n.w3.z, n.w3.w}, hiy[2] = {n.w4.x, n.w4.y}, hiz[2] = {n.w4.z, n.w4.w};
     const uint32_t meta[2] = {n.w1.z, n.w1.w};
     const bool nx = r.oct & 1u, ny = r.oct & 2u, nz = r.oct & 4u;
+    // a child's x and y plane distances as one .f32x2 add and fma and, with
+    // PAIR_Z (kernels with registers to spare), its near and far z distances
+    // as another; each half equals the scalar fma(q, scale, adj)
+    const uint64_t bias2 = f2_pack(-8388608.0f, -8388608.0f);
+    const uint64_t scxy = f2_pack(scx, scy), adjxy = f2_pack(adjx, adjy);
     uint32_t hits = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -226,12 +263,20 @@ __device__ __forceinline__ void isect_node(const Ray &r, const NodeWords &n, flo
         const uint32_t mx4 = meta[h] ^ (inner4 * r.oct);
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float tn = fmaxf(fmax3(tmin, __fmaf_rn(qbyte(nearx, b), scx, adjx),
-                                         __fmaf_rn(qbyte(neary, b), scy, adjy)),
-                                   __fmaf_rn(qbyte(nearz, b), scz, adjz));
-            const float tf = fminf(fmin3(tcur, __fmaf_rn(qbyte(farx, b), scx, adjx),
-                                         __fmaf_rn(qbyte(fary, b), scy, adjy)),
-                                   __fmaf_rn(qbyte(farz, b), scz, adjz));
+            float nxv, nyv, fxv, fyv, tn, tf;
+            f2_unpack(f2_fma(f2_add(qpair2_biased(nearx, neary, b), bias2), scxy, adjxy), nxv, nyv);
+            f2_unpack(f2_fma(f2_add(qpair2_biased(farx, fary, b), bias2), scxy, adjxy), fxv, fyv);
+            if constexpr (PAIR_Z) {
+                float nzv, fzv;
+                f2_unpack(f2_fma(f2_add(qpair2_biased(nearz, farz, b), bias2), f2_pack(scz, scz),
+                                 f2_pack(adjz, adjz)),
+                          nzv, fzv);
+                tn = fmaxf(fmax3(tmin, nxv, nyv), nzv);
+                tf = fminf(fmin3(tcur, fxv, fyv), fzv);
+            } else {
+                tn = fmaxf(fmax3(tmin, nxv, nyv), __fmaf_rn(qbyte(nearz, b), scz, adjz));
+                tf = fminf(fmin3(tcur, fxv, fyv), __fmaf_rn(qbyte(farz, b), scz, adjz));
+            }
             if (tn <= tf * kTfarScale) {
                 const uint32_t m = byte_of(mx4, b);
                 hits |= (m >> 5) << (m & 31u);

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(THREADS, ((MULTI || ANY) ? 1024 : 1152) / THRE
                     ++visits;
                     NodeWords nd = load_node(nodes, node);
                     uint32_t nh, ph;
-                    isect_node(r, nd, tmin, h.t, nh, ph);
+                    isect_node<ANY || MULTI>(r, nd, tmin, h.t, nh, ph);
                     if (STATS) n_nodes++;
                     const uint32_t pbase = nd.w1.y;
                     while (ph) {
