@@ -365,7 +365,11 @@ def run_ours(args) -> int:
                 "kernel": "k_trace_blas (closest hit)",
                 "bytes_per_ray": {"primary": round(bytes_p, 1), "incoherent": round(bytes_i, 1)},
                 "nodes_per_ray": {"primary": round(st_p[0], 3), "incoherent": round(st_i[0], 3)},
-                "tris_per_ray": {"primary": round(st_p[1], 3), "incoherent": round(st_i[1], 3)}}
+                "tris_per_ray": {"primary": round(st_p[1], 3), "incoherent": round(st_i[1], 3)},
+                # the pure ray I/O lower bound: 32 B ray in + 16 B hit out
+                "io_only": {"bytes_per_ray": BYTES_RAY_IO,
+                            "achieved": round(n_all * BYTES_RAY_IO / (ms_step * 1e-3) / 1e9, 1),
+                            "frac": round(n_all * BYTES_RAY_IO / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)}}
 
     # ---- shadow rays (any hit) toward a point light from primary hits
     hp = hits_p.cpu().numpy().view(np.float32).reshape(-1, 4)
