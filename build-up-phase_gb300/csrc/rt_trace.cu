@@ -394,6 +394,13 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
 
 }  // namespace
 
+// Refill threshold of the path tracer's queue traversals: a warp refills once
+// eight of its lanes are idle (2M box, 4 spp per call: 6.91 / 6.56 / 6.45 /
+// 6.43 ms per sample at 2 / 4 / 6 / 8; the ray-query calls keep the context's
+// batch_rays, whose default 4 is best for the soup's primary + incoherent
+// rays).  The batch's autotuner chose 8 as well.
+constexpr uint32_t kQueueRefill = 8u;
+
 // Queue-driven BLAS traversal for the wavefront path tracer: the ray count is
 // read on the device from *n_dev (at most max_n), the work counter is
 // `counter` (zeroed by the caller on the stream), and closest hits carry the
@@ -409,8 +416,7 @@ int launch_queue_trace(rt_context *ctx, cudaStream_t st, const uint8_t *accel, c
     a.hits_ext = nullptr;
     a.occluded = occluded;
     a.n = max_n;
-    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 4u;
-    if (a.refill > 32u) a.refill = 32u;
+    a.refill = kQueueRefill;
     a.err = ctx->d_err;
     a.stats = nullptr;
     a.n_dev = n_dev;
@@ -444,8 +450,7 @@ int launch_queue_trace_mixed(rt_context *ctx, cudaStream_t st, const uint8_t *ac
     a.rays2 = static_cast<const float4 *>(rays2);
     a.n_dev2 = n_dev2;
     a.n2 = max_n;
-    a.refill = ctx->tuning.batch_rays ? ctx->tuning.batch_rays : 4u;
-    if (a.refill > 32u) a.refill = 32u;
+    a.refill = kQueueRefill;
     a.err = ctx->d_err;
     a.out_rec = 1;
     a.counter = counter;

@@ -392,10 +392,16 @@ rt_status rt_trace_stats(rt_context *ctx, rt_stream stream, uint64_t accel,
 /* Tuning                                                                    */
 /* ------------------------------------------------------------------------ */
 
+/* Launch shape of the traversal kernel.  blocks_per_sm applies to every
+ * single-structure traversal (ray-query calls and rt_path_trace; any-hit
+ * launches use at most 8); batch_rays to the ray-query calls only -- the path
+ * tracer's queue traversals refill at 8 idle lanes, the batch uses its own
+ * autotuned shape.  Defaults: 128, 9, 4. */
 typedef struct rt_trace_tuning {
     uint32_t block_threads;   /* threads per block of the traversal kernel */
     uint32_t blocks_per_sm;   /* persistent blocks per SM                  */
-    uint32_t batch_rays;      /* rays a warp takes per work-stealing fetch  */
+    uint32_t batch_rays;      /* a warp refills its idle lanes (one atomic
+                                 fetch) once at least this many are idle    */
     uint32_t reserved;
 } rt_trace_tuning;
 rt_status rt_set_trace_tuning(rt_context *ctx, const rt_trace_tuning *t);
