@@ -333,7 +333,10 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
     float no[3] = {0, 0, 0}, nd[3] = {0, 0, 0};
     uint32_t p = 0, sid = 0;
     if (i < n) {
-        p = a.pidx_in[i];
+        p = __ldg(a.pidx_in + i);
+        // independent of the hit: issued before the dependent record loads
+        float4 T = a.tput[p];
+        const float4 hit = __ldg(a.hits + i);
         const uint8_t *accel = a.accel;
         const uint32_t *tri_material = a.tri_material;
         const rt_material *materials = a.materials;
@@ -362,10 +365,9 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
         float u[6];
         for (int k = 0; k < 6; ++k) u[k] = rtpt::pcg_uniform(g);
         a.rng[p] = g.state;
-        const float4 hit = a.hits[i];
         const uint32_t rec = __float_as_uint(hit.y);
         if (rec != 0xffffffffu) {
-            const float4 r0 = a.rays_in[2u * i], r1 = a.rays_in[2u * i + 1u];
+            const float4 r0 = __ldg(a.rays_in + 2u * i), r1 = __ldg(a.rays_in + 2u * i + 1u);
             const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
             const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(accel);
             const uint4 *pr = reinterpret_cast<const uint4 *>(accel + hd->prim_offset) + (size_t)rec * 3u;
@@ -386,13 +388,12 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
             if (len > 0.0f) {
                 for (int k = 0; k < 3; ++k) nrm[k] = ng[k] / len;
                 const float cosd = rtpt::dot3(nrm, d);
-                uint32_t mi = tri_material[tri];
+                uint32_t mi = __ldg(tri_material + tri);
                 if (mi >= n_materials) {
                     report_error(a.err, RT_ERR_BOUNDS, 0x80000000u | tri);
                     mi = 0;
                 }
                 const rt_material m = materials[mi];
-                float4 T = a.tput[p];
                 if (a.depth == 0 && cosd < 0.0f) {
                     float4 R = a.rad[p];
                     R.x = R.x + T.x * m.emission[0];
@@ -433,10 +434,10 @@ __device__ __forceinline__ void shade_one(const PtArgs &a, uint32_t i, uint32_t 
                         uint32_t lo = 0, hi = n_lights - 1u;
                         while (lo < hi) {  // first k with cdf[k] > target
                             uint32_t mid = (lo + hi) >> 1;
-                            if (light_cdf[mid] > target) hi = mid; else lo = mid + 1u;
+                            if (__ldg(light_cdf + mid) > target) hi = mid; else lo = mid + 1u;
                         }
                         const rt_pt_light L = lights[lo];
-                        const float4 ln = light_aux[lo];
+                        const float4 ln = __ldg(light_aux + lo);
                         const float su = sqrtf(u[1]);
                         const float b0 = 1.0f - su, b1 = u[2] * su;
                         const float b2 = (1.0f - b0) - b1;
