@@ -29,7 +29,11 @@ namespace rtc {
 namespace {
 
 constexpr int kTraceThreads = 128;  // block size of the single-structure kernels
-constexpr int kRing = 16;           // shared-memory stack entries per ray (single-structure kernels)
+// Shared-memory stack entries per ray of the single-structure kernels: 8 KB
+// per block, so nine blocks leave more of the SM's L1 to node fetches than
+// 16 entries did (1M soup: 2,150 -> 2,159 M rays/s; path tracer 6.33 -> 6.29
+// ms per sample); deeper entries spill to local memory.
+constexpr int kRing = 8;
 constexpr uint32_t kAnyBlocksPerSm = 1024u / kTraceThreads;  // resident blocks the any-hit kernel is bounded for
 constexpr int kMaxDepth = 64;       // total stack entries per ray
 constexpr uint32_t kNone = 0xffffffffu;
