@@ -90,11 +90,15 @@ struct BatchArgs {
 // path tracer traces a depth's shadow rays and the next depth's extension
 // rays together, so the two share one launch tail.
 // Register budget: the closest-hit and mixed single-structure kernels fit
-// nine 128-thread blocks per SM (56 registers, no spill; 36 warps against 32
-// at 64 registers: 2,093 -> 2,111 M rays/s on the 1M soup, 6.72 -> 6.58 ms
-// per path-traced sample).  The any-hit and multi-scene kernels keep eight
+// nine 128-thread blocks per SM (56 registers; 36 warps against 32 at 64
+// registers: 2,093 -> 2,111 M rays/s on the 1M soup, 6.72 -> 6.58 ms per
+// path-traced sample).  The any-hit and multi-scene kernels keep eight
 // blocks and 64 registers: any-hit shadow rays run 1,287 M rays/s there
 // against 1,202 at nine blocks, and the multi-scene kernels spill at 56.
+// The box test pairs the z planes too (isect_node<true>) where it pays: in
+// the 64-register kernels, and in the mixed kernel despite 20 bytes of spill
+// (path tracer 6.30 -> 6.23 ms per sample; the closest-hit kernel loses 2 %
+// with it).
 template <bool ANY, bool STATS, bool MULTI, int THREADS, int RING, bool MIXED = false>
 __global__ void __launch_bounds__(THREADS, ((MULTI || ANY) ? 1024 : 1152) / THREADS) k_trace_blas(const BatchArgs a) {
     static_assert((RING & (RING - 1)) == 0 && RING <= kMaxDepth, "RING is a power of two");
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(THREADS, ((MULTI || ANY) ? 1024 : 1152) / THRE
                     ++visits;
                     NodeWords nd = load_node(nodes, node);
                     uint32_t nh, ph;
-                    isect_node<ANY || MULTI>(r, nd, tmin, h.t, nh, ph);
+                    isect_node<ANY || MULTI || MIXED>(r, nd, tmin, h.t, nh, ph);
                     if (STATS) n_nodes++;
                     const uint32_t pbase = nd.w1.y;
                     while (ph) {
