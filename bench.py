@@ -391,6 +391,31 @@ def run_ours(args) -> int:
     ctx.sync(stream)
     shadow_mrays = len(sh) * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e6
 
+    # ---- the step's rays through a TLAS of one identity instance over the
+    # same BLAS (the sample's two-level layout): the persistent two-level walk
+    from rtcore.scenes import INSTANCE_DTYPE
+    inst = np.zeros(1, INSTANCE_DTYPE)
+    inst[0]["transform"] = np.eye(3, 4, dtype=np.float32)
+    inst[0]["custom_index_and_mask"] = 0xFF << 24
+    inst[0]["accel_ref"] = addr
+    d_inst = torch.from_numpy(inst.view(np.uint8)).to(dev)
+    tsz = ctx.tlas_sizes(1)
+    tl_accel = torch.empty(tsz.accel_bytes, dtype=torch.uint8, device=dev)
+    tl_scratch = torch.empty(tsz.scratch_bytes, dtype=torch.uint8, device=dev)
+    ctx.build_tlas(d_inst, 1, 0, tl_accel, tsz.accel_bytes, tl_scratch, tsz.scratch_bytes, stream)
+    tl_addr = ctx.address(tl_accel)
+    t_tl = []
+    for k in range(7):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.trace_closest(tl_addr, rays_all, hits_all, n_all, stream=stream)
+        e1.record(stream)
+        flush.fill_(k & 0xFF)
+        ctx.sync(stream)
+        if k >= 2:
+            t_tl.append(e0.elapsed_time(e1))
+    tlas_mrays = n_all / (statistics.median(t_tl) * 1e-3) / 1e6
+
     # ---- e2e: rays from pinned host memory, hits back to host
     hp_rays = torch.from_numpy(prim.view(np.uint8)).pin_memory()
     hi_rays = torch.from_numpy(inc.view(np.uint8)).pin_memory()
@@ -465,6 +490,7 @@ def run_ours(args) -> int:
                              "incoherent_mrays": round(n_i * k_split / (sum(t_i) * 1e-3) / 1e6, 2),
                              "separate_launches_mrays": round(n_all * k_split / ((sum(t_p) + sum(t_i)) * 1e-3) / 1e6, 2),
                              "shadow_anyhit_mrays": round(shadow_mrays, 2),
+                             "tlas_1instance_mrays": round(tlas_mrays, 2),
                              "build_ms": round(statistics.median(build_ms), 3),
                              "build_roofline": {
                                  "bytes_per_tri": BYTES_BUILD_PER_TRI,

@@ -7,7 +7,9 @@
 //
 //   k_trace_blas (rt_traverse.cuh)  persistent warps over a ray array
 //                   with atomic work stealing and a shared-memory stack ring.
-//   k_trace_tlas    two-level structures (instances): one ray per thread.
+//   k_trace_inst    two-level structures (instances): persistent warps as
+//                   above, a lane walking an instance's BLAS with its
+//                   object-space ray between TLAS steps.
 //                   Both kernels are launched; each returns at once when the
 //                   structure in the header is not its kind.
 //   k_pipeline      the sample's raygen + traceRayEXT + closest-hit / miss +
@@ -224,44 +226,270 @@ __device__ bool trace_ray(const uint8_t *accel, const float o[3], const float d[
 }
 
 
-// Two-level structures (instances): one ray per thread, grid-stride, through
-// the per-thread path.  Launched beside k_trace_blas; each kernel returns at
-// once when the structure is not its kind, so the host never reads it.
+// Two-level structures (instances), persistent like k_trace_blas: warps
+// refill idle lanes from the work counter, stacks live in a shared-memory
+// ring whose bottom spills to local memory.  At an instance a lane saves the
+// TLAS node's remaining work on its stack -- the node's internal children,
+// its instances not yet walked, then a return marker -- and walks the
+// instance's BLAS with the object-space ray; popping the marker restores the
+// world ray.  The visiting order is trace_ray's: a TLAS node's instances in
+// ascending record order, each BLAS in full, then the node's internal
+// children; closest hit = smallest t, ties broken by the smallest
+// (instance id, triangle) key.  Launched beside k_trace_blas; each kernel
+// returns at once when the structure is not its kind.
+constexpr uint32_t kInstGroup = 0x40000000u;   // stack entry: instances of a TLAS node still to walk
+constexpr uint32_t kReturnTop = 0x80000000u;   // stack entry: back to the TLAS
+constexpr int kInstDepth = 128;                // stack entries per ray (both levels)
+constexpr uint32_t kInstBlocksPerSm = 6;
+
+__device__ __forceinline__ bool inst_key_less(float t, uint32_t inst, uint32_t tri, const Hit &h) {
+    return t < h.t || (t == h.t && (!h.found || inst < h.inst || (inst == h.inst && tri < h.tri)));
+}
+
 template <bool ANY, bool STATS>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_tlas(const BatchArgs a) {
+__global__ void __launch_bounds__(kTraceThreads, kInstBlocksPerSm) k_trace_inst(const BatchArgs a) {
     const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
     if (hd->kind != RT_ACCEL_KIND_TLAS) return;
-    const int tid = threadIdx.x;
-    // Two-level structures: one ray per thread, grid-stride, through the
-    // per-thread path (instance transforms need a second ray setup).
-    unsigned long long st2[2] = {0ull, 0ull};
-    for (uint32_t i = blockIdx.x * blockDim.x + tid; i < a.n; i += gridDim.x * blockDim.x) {
-        const float4 r0 = __ldg(a.rays + 2u * i), r1 = __ldg(a.rays + 2u * i + 1u);
-        const float o[3] = {r0.x, r0.y, r0.z}, d[3] = {r1.x, r1.y, r1.z};
-        Hit th;
-        HitIds ids;
-        bool hit = trace_ray<ANY>(a.accel, o, d, r0.w, r1.w, 0xffu, th, ids, a.err, STATS ? st2 : nullptr);
-        if (ANY) {
-            if (a.occluded) a.occluded[i] = hit ? 1u : 0u;
-        } else {
-            float4 out = th.found ? make_float4(th.t, __uint_as_float(th.tri), th.u, th.v)
-                                  : make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
-            if (a.hits) a.hits[i] = out;
-            if (a.hits_ext) {
-                rt_hit_ext x;
-                x.t = out.x; x.u = out.z; x.v = out.w;
-                x.instance_id = th.found ? th.inst : kNone;
-                x.custom_index = th.found ? ids.custom : 0u;
-                x.geometry_index = th.found ? ids.geom : 0u;
-                x.primitive_id = th.found ? ids.prim : kNone;
-                x.sbt_record = th.found ? ids.sbt_off + ids.geom : 0u;
-                a.hits_ext[i] = x;
+    const uint4 *tnodes = reinterpret_cast<const uint4 *>(a.accel + hd->node_offset);
+    const uint4 *tprims = reinterpret_cast<const uint4 *>(a.accel + hd->prim_offset);
+    const uint32_t t_count = hd->node_count;
+    const bool t_empty = hd->prim_count == 0;
+    __shared__ uint2 s_stack[kRing][kTraceThreads];
+    const int tid = threadIdx.x, lane = tid & 31;
+
+    bool active = false, exhausted = false;
+    uint32_t ray_idx = 0;
+    float wo[3] = {0.f, 0.f, 0.f}, wd[3] = {0.f, 0.f, 0.f};  // the world ray
+    Ray r;  // the current level's ray
+    float tmin = 0.f;
+    Hit h;
+    h.t = 0.f; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.inst = 0; h.found = false;
+    uint32_t h_irec = kNone;  // TLAS record of the best hit's instance
+    uint32_t node = 0;
+    bool pending = false, in_blas = false;
+    const uint4 *bnodes = nullptr, *bprims = nullptr;
+    uint32_t b_count = 0, inst_id = 0, inst_rec = 0, visits_t = 0, visits_b = 0;
+    uint2 g = make_uint2(0u, 0u), ig = make_uint2(0u, 0u);
+    int sp = 0, lo = 0;
+    uint2 spill[kInstDepth];
+    unsigned long long n_nodes = 0, n_tris = 0;
+    const uint32_t n_rays = a.n;
+
+    auto push = [&](uint2 e) {
+        if (sp - lo == kRing) {
+            spill[lo] = s_stack[lo & (kRing - 1)][tid];
+            ++lo;
+        }
+        s_stack[sp & (kRing - 1)][tid] = e;
+        ++sp;
+    };
+
+    for (;;) {
+        // ---- refill idle lanes from the global counter
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= (int)a.refill) {
+            const uint32_t cnt = __popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.counter, cnt);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + cnt >= n_rays) exhausted = true;
+            if (!active) {
+                const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+                if (idx < n_rays) {
+                    const float4 r0 = __ldg(a.rays + 2u * idx), r1 = __ldg(a.rays + 2u * idx + 1u);
+                    wo[0] = r0.x; wo[1] = r0.y; wo[2] = r0.z;
+                    wd[0] = r1.x; wd[1] = r1.y; wd[2] = r1.z;
+                    ray_setup(r, wo, wd);
+                    tmin = r0.w;
+                    h.t = r1.w; h.u = 0.f; h.v = 0.f; h.rec = kNone; h.tri = kNone; h.inst = 0; h.found = false;
+                    h_irec = kNone;
+                    ray_idx = idx;
+                    active = true;
+                    in_blas = false;
+                    node = 0;
+                    pending = !t_empty;
+                    visits_t = 0;
+                    g = make_uint2(0u, 0u);
+                    ig = make_uint2(0u, 0u);
+                    sp = 0;
+                    lo = 0;
+                }
             }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        // ---- traversal steps until too many lanes are idle
+        for (;;) {
+            if (active) {
+                bool finish = false;
+                if (pending) {
+                    pending = false;
+                    const uint32_t count = in_blas ? b_count : t_count;
+                    const uint32_t visits = in_blas ? visits_b : visits_t;
+                    if (visits >= count || node >= count) {
+                        report_error(a.err, RT_ERR_BOUNDS, (in_blas ? 0x74000000u : 0x75000000u) | (node & 0xffffffu));
+                        finish = true;
+                    } else {
+                        if (in_blas) ++visits_b;
+                        else ++visits_t;
+                        NodeWords nd = load_node(in_blas ? bnodes : tnodes, node);
+                        uint32_t nh, ph;
+                        isect_node(r, nd, tmin, h.t, nh, ph);
+                        if (STATS) n_nodes++;
+                        g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
+                        if (!in_blas) {
+                            ig = make_uint2(nd.w1.y, ph);  // the node's instances, walked first
+                        } else {
+                            const uint32_t pbase = nd.w1.y;
+                            while (ph) {
+                                const uint32_t i = __ffs(ph) - 1;
+                                ph &= ph - 1u;
+                                const uint4 *rec = bprims + (size_t)(pbase + i) * 3u;
+                                const uint4 q0 = ldg4(rec), q1 = ldg4(rec + 1), q2 = ldg4(rec + 2);
+                                if (STATS) n_tris++;
+                                float t, u, v;
+                                if (!isect_tri(r,
+                                               make_float4(__uint_as_float(q0.x), __uint_as_float(q0.y),
+                                                           __uint_as_float(q0.z), 0.f),
+                                               make_float4(__uint_as_float(q1.x), __uint_as_float(q1.y),
+                                                           __uint_as_float(q1.z), 0.f),
+                                               make_float4(__uint_as_float(q2.x), __uint_as_float(q2.y),
+                                                           __uint_as_float(q2.z), 0.f),
+                                               tmin, h.t, t, u, v))
+                                    continue;
+                                if (ANY || inst_key_less(t, inst_id, q0.w, h)) {
+                                    h.t = t; h.u = u; h.v = v; h.rec = pbase + i; h.tri = q0.w; h.inst = inst_id;
+                                    h_irec = inst_rec;
+                                    h.found = true;
+                                }
+                                if (ANY) {
+                                    finish = true;
+                                    break;
+                                }
+                            }
+                        }
+                    }
+                }
+                // ---- next: an instance of the current TLAS node, else a node
+                while (!finish) {
+                    if (!in_blas && ig.y) {
+                        const uint32_t i = __ffs(ig.y) - 1;
+                        ig.y &= ig.y - 1u;
+                        const uint32_t rec = ig.x + i;
+                        const InstRec ir = load_inst(tprims, rec);
+                        if (((ir.cim >> 24) & 0xffu) == 0u) continue;  // masked out (cull mask 0xFF)
+                        const uint8_t *blas = reinterpret_cast<const uint8_t *>(ir.accel_ref);
+                        const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(blas);
+                        if (bh->prim_count == 0) continue;
+                        if (sp + 3 > kInstDepth) {
+                            report_error(a.err, RT_ERR_BOUNDS, 0x71000000u);
+                            finish = true;
+                            break;
+                        }
+                        // save the TLAS node's remaining work under a return marker
+                        if (g.y & 0xffu) push(g);
+                        if (ig.y) push(make_uint2(ig.x, ig.y | kInstGroup));
+                        push(make_uint2(0u, kReturnTop));
+                        g = make_uint2(0u, 0u);
+                        ig = make_uint2(0u, 0u);
+                        float o2[3], d2[3];
+                        xform_point(ir.w2o, wo, o2);
+                        xform_vector(ir.w2o, wd, d2);
+                        ray_setup(r, o2, d2);
+                        in_blas = true;
+                        bnodes = reinterpret_cast<const uint4 *>(blas + bh->node_offset);
+                        bprims = reinterpret_cast<const uint4 *>(blas + bh->prim_offset);
+                        b_count = bh->node_count;
+                        visits_b = 0;
+                        inst_id = ir.id;
+                        inst_rec = rec;
+                        node = 0;
+                        pending = true;
+                        break;
+                    }
+                    if (g.y & 0xffu) {
+                        const uint32_t k = __ffs(g.y & 0xffu) - 1;
+                        g.y &= ~(1u << k);
+                        const uint32_t s = k ^ r.oct;
+                        node = g.x + __popc((g.y >> 8) & ((1u << s) - 1u));
+                        pending = true;
+                        if (g.y & 0xffu) {
+                            if (sp >= kInstDepth) {
+                                report_error(a.err, RT_ERR_BOUNDS, in_blas ? 0x70000000u : 0x71000000u);
+                                finish = true;
+                                break;
+                            }
+                            push(g);
+                        }
+                        break;
+                    }
+                    if (sp == 0) { finish = true; break; }
+                    --sp;
+                    uint2 e;
+                    if (sp >= lo) {
+                        e = s_stack[sp & (kRing - 1)][tid];
+                    } else {
+                        e = spill[sp];
+                        lo = sp;
+                    }
+                    if (e.y & kReturnTop) {
+                        ray_setup(r, wo, wd);
+                        in_blas = false;
+                    } else if (e.y & kInstGroup) {
+                        ig = make_uint2(e.x, e.y & ~kInstGroup);
+                    } else {
+                        g = e;
+                    }
+                }
+                if (finish) {
+                    // ---- write the result
+                    if (ANY) {
+                        if (a.occluded) a.occluded[ray_idx] = h.found ? 1u : 0u;
+                    } else {
+                        const float4 out = h.found ? make_float4(h.t, __uint_as_float(h.tri), h.u, h.v)
+                                                   : make_float4(kInf, __uint_as_float(kNone), 0.f, 0.f);
+                        if (a.hits) a.hits[ray_idx] = out;
+                        if (a.hits_ext) {
+                            rt_hit_ext x;
+                            x.t = out.x; x.u = out.z; x.v = out.w;
+                            x.instance_id = h.found ? h.inst : kNone;
+                            x.custom_index = 0u;
+                            x.geometry_index = 0u;
+                            x.primitive_id = kNone;
+                            x.sbt_record = 0u;
+                            if (h.found) {
+                                const InstRec ir = load_inst(tprims, h_irec);
+                                const uint8_t *blas = reinterpret_cast<const uint8_t *>(ir.accel_ref);
+                                const rt_accel_header *bh = reinterpret_cast<const rt_accel_header *>(blas);
+                                const uint4 *bp = reinterpret_cast<const uint4 *>(blas + bh->prim_offset);
+                                x.custom_index = ir.cim & 0xffffffu;
+                                x.geometry_index = ldg4(bp + (size_t)h.rec * 3u + 1).w;
+                                x.primitive_id = ldg4(bp + (size_t)h.rec * 3u + 2).w;
+                                x.sbt_record = (ir.sof & 0xffffffu) + x.geometry_index;
+                            }
+                            a.hits_ext[ray_idx] = x;
+                        }
+                    }
+                    active = false;
+                    pending = false;
+                }
+            }
+            const uint32_t act = __ballot_sync(0xffffffffu, active);
+            if (act == 0u) break;
+            if (!exhausted && (uint32_t)__popc(~act) >= a.refill) break;
         }
     }
     if (STATS) {
-        atomicAdd(a.stats, st2[0]);
-        atomicAdd(a.stats + 1, st2[1]);
+        for (int o = 16; o > 0; o >>= 1) {
+            n_nodes += __shfl_xor_sync(0xffffffffu, n_nodes, o);
+            n_tris += __shfl_xor_sync(0xffffffffu, n_tris, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.stats, n_nodes);
+            atomicAdd(a.stats + 1, n_tris);
+        }
     }
 }
 
@@ -370,22 +598,23 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
     if (blocks > need) blocks = need;
     // Both kernels are launched; the one that does not match the structure's
     // kind returns immediately.
-    const uint32_t tl_blocks = (uint32_t)ctx->sm_count * 4u < need ? (uint32_t)ctx->sm_count * 4u : need;
+    uint32_t tl_blocks = kInstBlocksPerSm * (uint32_t)ctx->sm_count;
+    if (tl_blocks > need) tl_blocks = need;
     if (stats) {
         if (any) {
             k_trace_blas<true, true, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
-            k_trace_tlas<true, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_inst<true, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         } else {
             k_trace_blas<false, true, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
-            k_trace_tlas<false, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_inst<false, true><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         }
     } else {
         if (any) {
             k_trace_blas<true, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
-            k_trace_tlas<true, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_inst<true, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         } else {
             k_trace_blas<false, false, false, kTraceThreads, kRing><<<blocks, kTraceThreads, 0, st>>>(a);
-            k_trace_tlas<false, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
+            k_trace_inst<false, false><<<tl_blocks, kTraceThreads, 0, st>>>(a);
         }
     }
     RT_CUDA_CTX(ctx, cudaGetLastError());

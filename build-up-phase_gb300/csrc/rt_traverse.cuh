@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(THREADS, ((MULTI || ANY) ? 1024 : 1152) / THRE
     bool empty = true;
     if (!MULTI) {
         const rt_accel_header *hd = reinterpret_cast<const rt_accel_header *>(a.accel);
-        if (hd->kind != RT_ACCEL_KIND_BLAS) return;  // k_trace_tlas handles it
+        if (hd->kind != RT_ACCEL_KIND_BLAS) return;  // k_trace_inst handles it
         nodes = reinterpret_cast<const uint4 *>(a.accel + hd->node_offset);
         prims = reinterpret_cast<const uint4 *>(a.accel + hd->prim_offset);
         empty = hd->prim_count == 0;

@@ -103,6 +103,10 @@ def incoherent_rays(seed: int, n: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), t
     return rays
 
 
+# rt_instance: the bit layout of VkAccelerationStructureInstanceKHR (64 bytes)
+INSTANCE_DTYPE = np.dtype([("transform", "<f4", (3, 4)), ("custom_index_and_mask", "<u4"),
+                           ("sbt_offset_and_flags", "<u4"), ("accel_ref", "<u8")])
+
 # The reference sample's scene (vulkan-raytraced-triangle/main.cpp).
 REF8_VERTICES = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], np.float32)       # :676-681
 REF8_INDICES = np.array([[0, 1, 3], [1, 2, 3]], np.uint32)                                 # :682

@@ -103,6 +103,63 @@ def test_tlas_trace_ids(ctx, orc):
     np.testing.assert_array_equal(gpu_trace_stats(ctx, gt.addr, rays), so)
 
 
+def _instance_field(n, seed):
+    """n rotated, scaled and translated instances (ids 0..n-1): every 7th
+    masked out, pairs (10k, 10k+1) identical so their hits tie on t."""
+    from oracle import INSTANCE_DTYPE
+    rng = np.random.default_rng(seed)
+    inst = np.zeros(n, INSTANCE_DTYPE)
+    for k in range(n):
+        if k % 10 == 1:
+            inst[k] = inst[k - 1]
+        else:
+            ang = rng.uniform(0, 6.28)
+            s = rng.uniform(0.5, 2)
+            inst[k]["transform"] = np.array([[np.cos(ang) * s, -np.sin(ang) * s, 0, rng.uniform(-3, 3)],
+                                             [np.sin(ang) * s, np.cos(ang) * s, 0, rng.uniform(-3, 3)],
+                                             [0, 0, s, rng.uniform(-3, 3)]], np.float32)
+        mask = 0 if k % 7 == 3 else 0xFF
+        inst[k]["custom_index_and_mask"] = (k * 3) | (mask << 24)
+        inst[k]["sbt_offset_and_flags"] = (k % 4) | (1 << 24)
+    return inst
+
+
+@pytest.mark.parametrize("n_inst", [1, 37, 300])
+def test_tlas_instance_field_trace(ctx, orc, n_inst):
+    """The persistent two-level walk against the oracle: overlapping
+    instances of three BLASes (a soup, the sample's quads, an empty one),
+    masked and duplicated instances; hits, extended ids, occlusion and
+    traversal statistics bit for bit."""
+    import rtcore.scenes as S
+    items = [soup(3000, seed=5), ref8_items(), [(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32), None)]]
+    gb = [GpuBlas(ctx, it) for it in items]
+    ob = [orc.build_blas(it)[0] for it in items]
+    inst_g = _instance_field(n_inst, seed=n_inst)
+    inst_o = inst_g.copy()
+    which = [k % 3 if k % 11 else 2 for k in range(n_inst)]
+    for k in range(n_inst):
+        if k % 10 == 1:
+            which[k] = which[k - 1]  # the duplicate of instance k - 1, same BLAS
+    if n_inst == 1:
+        which = [1]
+    inst_g["accel_ref"] = [gb[w].addr for w in which]
+    inst_o["accel_ref"] = [ptr_of(ob[w]) for w in which]
+    gt = GpuTlas(ctx, inst_g)
+    ot, rc = orc.build_tlas(inst_o)
+    assert rc == 0
+    inc = S.incoherent_rays(77 + n_inst, 40000, (-4, -4, -4), (4, 4, 4), 1e30)
+    prim = orc.primary_rays(((0.0, 0.0, 12.0), 60.0), 160, 120, 0.0, 100.0)
+    rays = np.concatenate([inc, prim])
+    hg, xg = gpu_trace_closest(ctx, gt.addr, rays, ext=True)
+    ho, so, xo = orc.trace_closest(ot, rays, ext=True)
+    assert hg.tobytes() == ho.tobytes()
+    assert xg.tobytes() == xo.tobytes()
+    assert np.count_nonzero(hg["prim"] != 0xFFFFFFFF) > 500
+    np.testing.assert_array_equal(gpu_trace_any(ctx, gt.addr, rays), orc.trace_any(ot, rays)[0])
+    np.testing.assert_array_equal(gpu_trace_stats(ctx, gt.addr, rays), so)
+    np.testing.assert_array_equal(gpu_trace_stats(ctx, gt.addr, rays, any_hit=True), orc.trace_any(ot, rays)[1])
+
+
 def _pipeline_image(ctx, accel_addr, camera, w, h, chit, sbt_colors=None):
     import rtcore
     import torch
