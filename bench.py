@@ -61,8 +61,8 @@ BYTES_TRI = 36      # FP32 vertex triplet
 # its refit, 80 / 8 for the BVH8 node share of one leaf-equivalent
 BYTES_BUILD_PER_TRI = 48 + 12 + 24 * 8 + 2 * 24 + 80 // 8
 # DRAM bytes (read + write) of one step's traversal launch measured by ncu
-# (cold caches): 434.3 MB read + 66.9 MB written
-TRAFFIC_BYTES_PER_STEP = 501_200_000
+# (cold caches): 436.9 MB read + 68.0 MB written
+TRAFFIC_BYTES_PER_STEP = 504_800_000
 
 
 def _env_int(name: str, default: int) -> int:
