@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kTraceThreads, kInstBlocksPerSm) k_trace_inst(
                         else ++visits_t;
                         NodeWords nd = load_node(in_blas ? bnodes : tnodes, node);
                         uint32_t nh, ph;
-                        isect_node(r, nd, tmin, h.t, nh, ph);
+                        isect_node<true>(r, nd, tmin, h.t, nh, ph);
                         if (STATS) n_nodes++;
                         g = make_uint2(nd.w1.x, nh | ((nd.w0.w >> 24) << 8));
                         if (!in_blas) {
