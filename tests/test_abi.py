@@ -83,3 +83,15 @@ def test_ppm_and_pfm_writers(rtlib, tmp_path):
     assert body.startswith(hdr)
     f = np.frombuffer(body[len(hdr):], np.float32).reshape(2, 3, 3)
     assert np.array_equal(f[1, 0], img[0, 0, :3])  # bottom row first
+
+
+def test_python_record_layouts_match_the_headers():
+    """The numpy mirrors of rt_ray, rt_hit, rt_hit_ext and rt_instance (the
+    bit layout of VkAccelerationStructureInstanceKHR) have the C sizes and
+    agree with the oracle's, field for field."""
+    import oracle
+    import rtcore.scenes as S
+    assert S.INSTANCE_DTYPE.itemsize == 64
+    assert S.INSTANCE_DTYPE == oracle.INSTANCE_DTYPE
+    assert S.RAY_DTYPE.itemsize == 32 and S.HIT_EXT_DTYPE.itemsize == 32
+    assert S.INSTANCE_DTYPE.fields["accel_ref"][1] == 56
