@@ -630,7 +630,8 @@ int launch_batch(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray 
 // eight of its lanes are idle (2M box, 4 spp per call: 6.91 / 6.56 / 6.45 /
 // 6.43 ms per sample at 2 / 4 / 6 / 8; the ray-query calls keep the context's
 // batch_rays, whose default 4 is best for the soup's primary + incoherent
-// rays).  The batch's autotuner chose 8 as well.
+// rays; re-checked with the packed box test and the 8-entry ring: 6.26 /
+// 6.23 / 6.33 ms at 6 / 8 / 12).  The batch's autotuner chose 8 as well.
 constexpr uint32_t kQueueRefill = 8u;
 
 // Queue-driven BLAS traversal for the wavefront path tracer: the ray count is
