@@ -35,8 +35,9 @@ __device__ __forceinline__ bool key_less(float t, uint64_t key, float bt, uint64
 }
 
 // ---------------------------------------------------------------------------
-// Simple per-thread traversal (local-memory stack): two-level and pipeline
-// paths.  Same visiting order as the persistent kernel.
+// Simple per-thread traversal (local-memory stack) for the sample pipeline
+// (k_pipeline): one thread per pixel, both structure kinds.  Same visiting
+// order as the persistent kernels.
 // ---------------------------------------------------------------------------
 
 struct LocalStack {
