@@ -211,3 +211,55 @@ def test_scene_generators_deterministic(rtlib):
     r = S.incoherent_rays(1, 1000)
     n = np.linalg.norm(r["dir"], axis=1)
     assert np.abs(n - 1).max() < 1e-6
+
+
+def test_tlas_walk_matches_flattened_geometry(orc):
+    """The oracle's two-level walk against one world-space BLAS of the same
+    instances: each unmasked instance's triangles transformed to world space
+    as one geometry.  Object-space and world-space arithmetic round
+    differently, so the check is the hit's identity -- which instance and
+    which triangle, hit or miss -- on all but grazing rays, and t to 1e-4 of
+    max(t, 1)."""
+    import rtcore.scenes as S
+    from oracle import INSTANCE_DTYPE
+    v, i, _, _ = S.box(17, 3, 4)  # closed box walls and three small spheres
+    blas, rc = orc.build_blas([(v, i, None)])
+    assert rc == 0
+    rng = np.random.default_rng(5)
+    n_inst = 24
+    inst = np.zeros(n_inst, INSTANCE_DTYPE)
+    world_items, geom_of = [], {}
+    for k in range(n_inst):
+        ang = rng.uniform(0, 6.28)
+        s = rng.uniform(0.5, 2.0)
+        m = np.array([[np.cos(ang) * s, -np.sin(ang) * s, 0, rng.uniform(-2, 2)],
+                      [np.sin(ang) * s, np.cos(ang) * s, 0, rng.uniform(-2, 2)],
+                      [0, 0, s, rng.uniform(-2, 2)]], np.float32)
+        mask = 0 if k % 5 == 2 else 0xFF
+        inst[k]["transform"] = m
+        inst[k]["custom_index_and_mask"] = k | (mask << 24)
+        inst[k]["accel_ref"] = ptr_of(blas)
+        if mask:
+            wv = (v.astype(np.float64) @ m[:, :3].T.astype(np.float64) + m[:, 3]).astype(np.float32)
+            geom_of[len(world_items)] = k
+            world_items.append((wv, i, None))
+    tlas, rc = orc.build_tlas(inst)
+    assert rc == 0
+    flat, rc = orc.build_blas(world_items)
+    assert rc == 0
+    rays = np.concatenate([S.incoherent_rays(23, 20000, (-3, -3, -3), (3, 3, 3), 1e30),
+                           orc.primary_rays(((0.0, 0.0, 8.0), 60.0), 120, 90, 0.0, 100.0)])
+    ht, _, xt = orc.trace_closest(tlas, rays, ext=True)
+    hf, _, xf = orc.trace_closest(flat, rays, ext=True)
+    hit_t, hit_f = ht["prim"] != 0xFFFFFFFF, hf["prim"] != 0xFFFFFFFF
+    assert hit_t.sum() > 2000
+    assert np.mean(hit_t == hit_f) >= 0.999
+    both = np.nonzero(hit_t & hit_f)[0]
+    inst_f = np.array([geom_of[g] for g in xf["geometry_index"][both]])
+    same = (xt["instance_id"][both] == inst_f) & (xt["primitive_id"][both] == xf["primitive_id"][both])
+    assert np.mean(same) >= 0.999
+    assert not np.isin(xt["instance_id"][hit_t], [k for k in range(n_inst) if k % 5 == 2]).any()
+    agree = both[same]
+    # t error relative to max(t, 1): rays that start on a wall have t ~ 0
+    rel = np.abs(ht["t"][agree] - hf["t"][agree]) / np.maximum(np.abs(hf["t"][agree]), 1.0)
+    assert np.quantile(rel, 0.999) <= 1e-4
