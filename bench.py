@@ -18,14 +18,23 @@ Prints one JSON line.  Besides the headline value it reports:
   roofline      achieved algorithmic GB/s of the traversal kernel (rays x
                 (48 B ray I/O + 80 B x nodes visited + 36 B x triangles
                 tested), counts from the instrumented kernel) over measured
-                HBM bandwidth
+                HBM bandwidth; beside it the step's L2 traffic over the L2
+                read bandwidth measured in the same run, and the issue-slot
+                bound (warp instructions per ray at the sampled SM clock)
   cpu_baseline  the CPU oracle (same BVH8, same traversal, all host threads)
-                on a bounded sample of the same rays
+                timed by the reference arm's function on all of the step's
+                rays
   shadow/build  any-hit shadow-ray Mrays/s and BVH build ms (not in value)
+  secondary     the 2M-triangle box scene, the path tracer, the MLP cache,
+                the 64-scene batch and (relmse) the equal-time relMSE of the
+                learned form against the plain path tracer on the 8M-triangle
+                box against a 16,384-spp reference (--no-relmse skips it)
   clocks        nvidia-smi samples taken during the timed region
 --impl reference times the CPU implementation (the oracle port: the
 reference's own ray tracing runs in a Vulkan driver, which does not exist on
-this machine) on the same workload and prints the same line.
+this machine) on the same workload and config, all 4,147,200 rays per step,
+with inputs from the oracle's own generators (the product library is not
+loaded), and prints the same line.
 """
 from __future__ import annotations
 
@@ -50,6 +59,7 @@ N_TRIS = 1_000_000
 W, H = 1920, 1080
 CAMERA = ((0.5, 0.5, 2.5), 60.0)
 LIGHT = (0.5, 2.0, 0.5)
+SEED_BASE = 0x5EED0000   # seeded workloads: 0x5EED0000 + workload number (2: the soup)
 METRIC = "Mrays/s primary+incoherent (closest hit), 1M-triangle soup, 1920x1080 each"
 WORKLOAD = "triangle soup 1M tris (unit cube, edges U(0.001,0.02)); 1920x1080 primary + 1920x1080 incoherent rays"
 BYTES_RAY_IO = 48   # 32 B ray in + 16 B hit out
@@ -63,6 +73,22 @@ BYTES_BUILD_PER_TRI = 48 + 12 + 24 * 8 + 2 * 24 + 80 // 8
 # DRAM bytes (read + write) of one step's traversal launch measured by ncu
 # (cold caches): 436.9 MB read + 68.0 MB written
 TRAFFIC_BYTES_PER_STEP = 504_800_000
+# From the same ncu capture of the step's launch: L2 sectors (32 B) moved,
+# warp instructions issued and the SIMT efficiency (active threads per warp
+# instruction / 32)
+L2_SECTORS_PER_STEP = 235_000_000
+WARP_INST_PER_STEP = 1_861_000_000
+SIMT_EFFICIENCY = 16.5 / 32
+TRAFFIC_SOURCE = "constant from one ncu capture of the step's launch (cold caches), not measured in this run"
+SMS, SMSP_PER_SM = 152, 4   # GB300: 152 SMs, four schedulers (one warp instruction per cycle each)
+L2_NOTE = ("GPU arm: L2 flushed between steps (256 MB write, outside the step events); "
+           "CPU arm: no cache flush, every step traces all 4.15M rays (133 MB of rays, 71 MB of BVH)")
+
+
+def config(world: int) -> dict:
+    """The workload's config, the same in both arms."""
+    return {"workload": WORKLOAD, "tris": N_TRIS, "rays_per_step": 2 * W * H,
+            "parallelism": f"replicas{world}" if world > 1 else "single", "l2": L2_NOTE}
 
 
 def _env_int(name: str, default: int) -> int:
@@ -160,11 +186,24 @@ def primary_rays_np():
 
 
 def workload():
+    """The GPU arm's inputs, from the library's seeded generators."""
     import rtcore.scenes as S
-    seed = S.SEED_BASE + 2
+    seed = SEED_BASE + 2
     v, i = S.soup(seed, N_TRIS)
     prim = primary_rays_np()
     inc = S.incoherent_rays(seed, W * H, (0, 0, 0), (1, 1, 1), 1e30)
+    return v, i, prim, inc
+
+
+def workload_cpu():
+    """The same inputs (byte for byte: tests/test_pt_oracle.py) from the
+    oracle's restatement of the generators, so that the CPU arm loads nothing
+    of the product library."""
+    import oracle
+    seed = SEED_BASE + 2
+    v, i = oracle.scene_soup(seed, N_TRIS)
+    prim = oracle.primary_rays(CAMERA, W, H, 0.0, 100.0)
+    inc = oracle.incoherent_rays(seed, W * H, (0, 0, 0), (1, 1, 1), 1e30)
     return v, i, prim, inc
 
 
@@ -172,19 +211,24 @@ def workload():
 # CPU side (oracle port): the reference arm and the cpu_baseline leg
 # ---------------------------------------------------------------------------
 
-def cpu_trace_rate(v, i, prim, inc, n_sample: int, threads: int = 0, repeats: int = 1):
-    """Mrays/s of the oracle's BVH8 closest-hit traversal (all host threads)
-    on the first n_sample rays of each set."""
+def cpu_trace_rate(v, i, rays, warmup: int, steps: int, threads: int = 0):
+    """Mrays/s of the oracle's BVH8 closest-hit traversal on all host threads:
+    `warmup` untimed calls over all of `rays`, then `steps` timed calls.  Both
+    CPU figures (the reference arm and the GPU arm's cpu_baseline) come from
+    this function on the step's full 4,147,200 rays.  Returns (Mrays/s,
+    seconds per step, threads, the oracle structure)."""
     import oracle
     accel, rc = oracle.build_blas([(v, i, None)])
-    rays = np.concatenate([prim[:: max(1, len(prim) // n_sample)][:n_sample],
-                           inc[:n_sample]])
-    times = []
-    for _ in range(repeats):
-        t0 = time.perf_counter()
+    if rc != 0:
+        raise RuntimeError(f"oracle build failed: {rc}")
+    threads = threads or oracle.hw_threads()
+    for _ in range(warmup):
         oracle.trace_closest(accel, rays, threads)
-        times.append(time.perf_counter() - t0)
-    return len(rays) / min(times) / 1e6, len(rays), (threads or oracle.hw_threads())
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.trace_closest(accel, rays, threads)
+    dt = (time.perf_counter() - t0) / max(1, steps)
+    return len(rays) / dt / 1e6, dt, threads, accel
 
 
 def whole_job(ms_step: float, units_per_rank: int, world: int, device=None):
@@ -202,33 +246,30 @@ def whole_job(ms_step: float, units_per_rank: int, world: int, device=None):
 
 
 def run_reference(args) -> int:
-    rank = _env_int("RANK", 0)
+    """The reference arm: the CPU restatement of the path (the reference's own
+    ray tracing runs inside a Vulkan driver on RT cores, and no Vulkan stack
+    exists on this machine) on the same workload, every step all 4,147,200
+    rays, with inputs made by the oracle's own generators."""
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
     if rank != 0:
         return 0
-    import oracle
-    v, i, prim, inc = workload()
-    accel, rc = oracle.build_blas([(v, i, None)])
-    n = 250_000
-    rays = np.concatenate([prim[:: len(prim) // n][:n], inc[:n]])
-    threads = oracle.hw_threads()
-    for _ in range(args.warmup):
-        oracle.trace_closest(accel, rays[:20000], threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle.trace_closest(accel, rays, threads)
-    dt = time.perf_counter() - t0
-    value = len(rays) * args.steps / dt / 1e6
-    sample = f"{n} primary (strided) + {n} incoherent rays of the workload per step"
+    v, i, prim, inc = workload_cpu()
+    rays = np.concatenate([prim, inc])
+    value, dt, threads, accel = cpu_trace_rate(v, i, rays, args.warmup, args.steps)
+    hdr = accel[:256]
+    sample = f"all {len(rays)} rays of the workload per step (2073600 primary + 2073600 incoherent)"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "tris": N_TRIS, "rays_per_step": len(rays)},
+            "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG32 scene and rays)",
+            "config": config(world),
             "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "bvh": {"nodes": int(hdr[16:20].view(np.uint32)[0]), "depth": int(hdr[32:36].view(np.uint32)[0])},
             "note": "the reference's ray tracing runs inside a Vulkan driver on RT cores; no Vulkan stack exists "
-                    "on this machine, so the CPU port of the same algorithm (oracle/) is timed"}
+                    "on this machine, so the CPU port of the same algorithm (oracle/: same BVH8, same traversal "
+                    "order) is timed on all host threads"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -354,12 +395,13 @@ def run_ours(args) -> int:
     peaks = _peaks()
     alg_bytes = n_p * bytes_p + n_i * bytes_i
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    l2_gbs = l2_read_bandwidth(ctx, stream, dev)
+    l2_traffic = L2_SECTORS_PER_STEP * 32
+    warp_inst_per_ray = WARP_INST_PER_STEP / n_all
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4),
-                # dram__bytes_read.sum + dram__bytes_write.sum of the step's
-                # launch, from one ncu capture of this workload
-                # (cold caches): profiles/k_trace_blas_soup1M_1920x1080.md
                 "traffic": TRAFFIC_BYTES_PER_STEP,
+                "traffic_source": TRAFFIC_SOURCE,
                 "algorithmic_bytes_per_step": round(alg_bytes),
                 "peak_source": peaks["source"],
                 "kernel": "k_trace_blas (closest hit)",
@@ -369,7 +411,17 @@ def run_ours(args) -> int:
                 # the pure ray I/O lower bound: 32 B ray in + 16 B hit out
                 "io_only": {"bytes_per_ray": BYTES_RAY_IO,
                             "achieved": round(n_all * BYTES_RAY_IO / (ms_step * 1e-3) / 1e9, 1),
-                            "frac": round(n_all * BYTES_RAY_IO / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)}}
+                            "frac": round(n_all * BYTES_RAY_IO / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)},
+                # the BVH stays in L2: the step's L2 traffic over the L2 read
+                # bandwidth measured in this run (a 64 MB buffer read repeatedly)
+                "l2": {"achieved": round(l2_traffic / (ms_step * 1e-3) / 1e9, 1), "peak": round(l2_gbs, 1),
+                       "unit": "GB/s", "frac": round(l2_traffic / (ms_step * 1e-3) / 1e9 / l2_gbs, 4),
+                       "traffic_per_step": l2_traffic, "traffic_source": TRAFFIC_SOURCE,
+                       "peak_source": "measured in this run: 64 MB buffer resident in L2, 16-byte L1-bypassing "
+                                      "loads, CUDA events"},
+                # issue slots: the kernel's warp instructions per ray against
+                # one warp instruction per scheduler per cycle at the sampled clock
+                "issue": None}
 
     # ---- shadow rays (any hit) toward a point light from primary hits
     hp = hits_p.cpu().numpy().view(np.float32).reshape(-1, 4)
@@ -458,23 +510,32 @@ def run_ours(args) -> int:
     e2e_value = n_all * world / (e2e_ms * 1e-3) / 1e6
 
     extra = secondary_workloads(ctx, stream, dev) if (rank == 0 and not args.no_secondary) else {}
+    if rank == 0 and not args.no_relmse:
+        extra["relmse"] = relmse_workload(ctx, args.relmse_ref_spp, args.relmse_budget_ms)
 
     out = None
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            cv, cn, cores = cpu_trace_rate(v, i, prim, inc, 100_000)
+            cv, _, cores, _ = cpu_trace_rate(v, i, np.concatenate([prim, inc]), 1, 3)
             cpu = {"value": round(cv, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                   "sample": f"{cn} rays (100000 strided primary + 100000 incoherent) of the workload, oracle BVH8 "
-                             f"traversal on {cores} host threads"}
+                   "sample": f"all {n_all} rays of the workload per step, 1 warm-up + 3 timed steps, oracle BVH8 "
+                             f"traversal on {cores} host threads (the reference arm's function)"}
+        clk = clocks.summary()
+        mhz = clk.get("sm_mhz") or 2070.0
+        issue_rate = SMS * SMSP_PER_SM * mhz * 1e6 / warp_inst_per_ray / 1e6  # M rays/s at full issue
+        roofline["issue"] = {"achieved": round(value / world, 1), "peak": round(issue_rate, 1), "unit": "Mrays/s",
+                             "frac": round(value / world / issue_rate, 4),
+                             "warp_instructions_per_ray": round(warp_inst_per_ray, 1),
+                             "simt_efficiency": round(SIMT_EFFICIENCY, 3),
+                             "peak_all_lanes_active": round(issue_rate / SIMT_EFFICIENCY, 1),
+                             "sm_mhz": mhz, "source": "warp instructions and SIMT efficiency: " + TRAFFIC_SOURCE}
         out = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
                "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms_step, 4),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded PCG32 scene and rays)",
-               "config": {"workload": WORKLOAD, "tris": N_TRIS, "rays_per_step": n_all,
-                          "parallelism": f"replicas{world}" if world > 1 else "single",
-                          "l2": "flushed between steps (256 MB write, outside the step events)",
-                          "bvh_nodes": n_nodes, "bvh_depth": depth},
+               "config": config(world),
+               "bvh": {"nodes": n_nodes, "depth": depth},
                "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",
                        "h2d_bytes_per_step": n_all * 32, "d2h_bytes_per_step": n_all * 16,
                        "transfer": "rt_trace_closest_host on pinned host buffers: the traversal launch reads "
@@ -500,12 +561,28 @@ def run_ours(args) -> int:
                                  "note": "latency-bound: 13 dependent kernels, the collapse a cooperative grid of level barriers"},
                              "wall_s_timed_region": round(t_wall, 3)},
                "secondary": extra,
-               "clocks": clocks.summary()}
+               "clocks": clk}
         print(json.dumps(out), flush=True)
     ctx.close()
     if dist:
         tdist.destroy_process_group()
     return 0
+
+
+def l2_read_bandwidth(ctx, stream, dev, mbytes: int = 64, passes: int = 40) -> float:
+    """GB/s of reading an L2-resident buffer (64 MB, below the 129 MB L2):
+    rt_debug_read_sweep reads it `passes` times per launch with 16-byte
+    loads that bypass L1; best of five launches after a warm-up, CUDA events
+    on the launching stream."""
+    import torch
+    buf = torch.ones(mbytes << 20, dtype=torch.uint8, device=dev)
+    ctx.read_sweep(buf, buf.numel(), passes, stream)
+    best = None
+    for _ in range(5):
+        ms = _events(torch, stream, lambda: ctx.read_sweep(buf, buf.numel(), passes, stream), 1)
+        best = ms if best is None else min(best, ms)
+    ctx.sync(stream)
+    return buf.numel() * passes / (best * 1e-3) / 1e9
 
 
 def _events(torch, stream, fn, reps: int) -> float:
@@ -615,6 +692,36 @@ def secondary_workloads(ctx, stream, dev) -> dict:
     return out
 
 
+def relmse_workload(ctx, ref_spp: int, budget_ms: float) -> dict:
+    """The second half of the metric: equal-time relMSE of the learned form
+    (MLP radiance cache ending paths at their second vertex) against the
+    plain path tracer, on the learned workload -- the box with 160 icospheres
+    (8,000,014 triangles), 1920x1080, depth 8, Russian roulette from 3,
+    65,536 training paths per sample in Adam batches of 16,384 (lr 1e-3),
+    four samples per call for both forms -- measured against a plain
+    reference of ref_spp samples per pixel.  Reports each form's curve, the
+    relMSE both reach in the same time, and the time each needs to reach
+    relMSE 1e-3 on the CUDA-event clock and the wall clock; the target is a
+    learned/plain time ratio of at most 0.5."""
+    from rtcore.relmse import GpuBox, equal_time, reference
+    t0 = time.perf_counter()
+    box = GpuBox(ctx, 160, 50)
+    t1 = time.perf_counter()
+    ref = reference(ctx, box, W, H, ref_spp)
+    t2 = time.perf_counter()
+    res = equal_time(ctx, box, W, H, ref, budget_ms, target=1e-3, train_paths=65536, train_batch=16384, lr=1e-3,
+                     spp_per_call=4)
+    ratio = res["time_to_target_wall_ms"]["ratio_cached_over_plain"]
+    out = {"workload": "box scene, 160 icospheres (8,000,014 triangles), 1920x1080, depth 8, RR from 3",
+           "tris": box.n_tris, "reference_spp": ref_spp, "reference_wall_s": round(t2 - t1, 1),
+           "setup_wall_s": round(t1 - t0, 1), "budget_gpu_ms": budget_ms, "train_paths": 65536,
+           "train_batch": 16384, "lr": 1e-3, "spp_per_call": 4, "target_relmse": 1e-3,
+           "target_time_ratio": 0.5,
+           "meets_target": bool(ratio is not None and ratio <= 0.5)}
+    out.update(res)
+    return out
+
+
 def batch_workload(ctx, stream, dev) -> dict:
     """The batched form: 64 seeded scenes (lit soups and box scenes of
     10k-5M triangles, 512^2-2048^2 pixels, own cameras), 16 spp, depth 8:
@@ -670,6 +777,11 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--no-secondary", action="store_true", help="skip the box-scene / path-tracer / MLP figures")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the learned form's equal-time relMSE block")
+    ap.add_argument("--relmse-ref-spp", type=int, default=16384,
+                    help="samples per pixel of the plain reference image of the relMSE block")
+    ap.add_argument("--relmse-budget-ms", type=float, default=12000.0,
+                    help="GPU time given to each form in the relMSE block")
     args = ap.parse_args(argv)
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

@@ -1576,6 +1576,12 @@ int static_scratch_address(rt_context *ctx, void **out) {
 }
 
 }  // namespace
+
+void static_scratch_forget(int device) {
+    if (device >= 0 && device < kStaticScratchDevices)
+        __atomic_store_n(&g_static_scratch_addr[device], (void *)nullptr, __ATOMIC_RELEASE);
+}
+
 }  // namespace rtc
 
 extern "C" rt_status rt_build_blas_static_scratch(rt_context *ctx, rt_stream stream,
@@ -1588,32 +1594,19 @@ extern "C" rt_status rt_build_blas_static_scratch(rt_context *ctx, rt_stream str
     if ((flags & RT_BUILD_MORTON30) && (flags & RT_BUILD_MORTON63))
         return set_error(ctx, RT_ERR_INVALID_ARG, "RT_BUILD_MORTON30 and RT_BUILD_MORTON63 are exclusive");
     static thread_local GeomParams gp;
-    std::memset(&gp, 0, sizeof(gp));
-    gp.n_geoms = n_geoms;
     uint64_t total = 0;
-    for (uint32_t g = 0; g < n_geoms; ++g) {
-        const rt_geometry_triangles &G = geoms[g];
-        if (G.tri_count && (!G.vertices || G.vertex_stride < 12u ||
-                            (G.index_type != RT_INDEX_UINT32 && G.index_type != RT_INDEX_NONE) ||
-                            (G.index_type == RT_INDEX_UINT32 && !G.indices)))
-            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas_static_scratch: bad geometry descriptor");
-        if (G.index_type == RT_INDEX_NONE && G.tri_count && (uint64_t)G.tri_count * 3u - 1u > G.max_vertex)
-            return set_error(ctx, RT_ERR_INVALID_ARG, "rt_build_blas_static_scratch: non-indexed geometry exceeds max_vertex");
-        gp.table[g] = (uint32_t)total;
-        gp.g[g] = G;
-        total += G.tri_count;
-    }
+    int rc = geom_params(ctx, geoms, n_geoms, gp, total, "rt_build_blas_static_scratch: bad geometry descriptor");
+    if (rc) return rc;
     if (total > RT_STATIC_SCRATCH_MAX_TRIS)
         return set_error(ctx, RT_ERR_UNSUPPORTED,
                          "rt_build_blas_static_scratch: more than RT_STATIC_SCRATCH_MAX_TRIS (131072) triangles; "
                          "use rt_build_blas with a caller-allocated scratch buffer");
-    gp.table[n_geoms] = (uint32_t)total;
     const int passes = (flags & RT_BUILD_MORTON30) ? 4 : 8;
     const BuildLayout L = build_layout((uint32_t)total, 48u, passes);
     if (L.total > kStaticScratchBytes)
         return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_build_blas_static_scratch: scratch layout exceeds the static array");
     void *scratch = nullptr;
-    int rc = static_scratch_address(ctx, &scratch);
+    rc = static_scratch_address(ctx, &scratch);
     if (rc) return rc;
     BuildCall bc{RT_ACCEL_KIND_BLAS, (uint32_t)total, 48u, n_geoms, flags};
     return run_build(ctx, static_cast<cudaStream_t>(stream), bc, &gp, nullptr, accel, accel_bytes, scratch,

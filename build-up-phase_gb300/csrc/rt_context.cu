@@ -39,7 +39,46 @@ uint32_t *acquire_counter(rt_context *ctx, cudaStream_t stream) {
 
 }  // namespace rtc
 
+namespace rtc {
+namespace {
+
+// Bandwidth probe: reads the buffer `passes` times, four independent 16-byte
+// loads per thread and step, cached in L2 only (ld.global.cg), so that a
+// buffer smaller than L2 measures L2 read bandwidth and a larger one HBM.
+// The XOR of everything read decides one store nobody expects, which keeps
+// the loads alive.
+__global__ void __launch_bounds__(512) k_read_sweep(const uint4 *__restrict__ buf, uint64_t n16, uint32_t passes,
+                                                    uint32_t *sink) {
+    uint32_t acc = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t r = 0; r < passes; ++r) {
+        uint64_t i = t;
+        for (; i + 3u * stride < n16; i += 4u * stride) {
+            const uint4 a = __ldcg(buf + i), b = __ldcg(buf + i + stride);
+            const uint4 c = __ldcg(buf + i + 2u * stride), d = __ldcg(buf + i + 3u * stride);
+            acc ^= (a.x ^ b.y) ^ (c.z ^ d.w);
+        }
+        for (; i < n16; i += stride) acc ^= __ldcg(buf + i).x;
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;
+}
+
+}  // namespace
+}  // namespace rtc
+
 using namespace rtc;
+
+extern "C" rt_status rt_debug_read_sweep(rt_context *ctx, rt_stream stream, const void *buf, uint64_t bytes,
+                                         uint32_t passes) {
+    if (!ctx || (bytes && !buf) || (bytes & 15u) || (reinterpret_cast<uintptr_t>(buf) & 15u))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_debug_read_sweep: a 16-byte aligned buffer of 16-byte units");
+    if (bytes == 0 || passes == 0) return RT_OK;
+    k_read_sweep<<<(unsigned)ctx->sm_count * 4u, 512, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const uint4 *>(buf), bytes / 16u, passes, ctx->d_counters + kNumCounters);
+    RT_CUDA_CTX(ctx, cudaGetLastError());
+    return RT_OK;
+}
 
 extern "C" uint32_t rt_abi_version(void) { return RTCORE_ABI_VERSION; }
 
@@ -52,6 +91,7 @@ extern "C" rt_status rt_context_create(int device, rt_context **out) {
     rt_context *ctx = new (std::nothrow) rt_context();
     if (!ctx) return RT_ERR_OOM;
     ctx->device = device;
+    static_scratch_forget(device);
     cudaError_t e = cudaSetDevice(device);
     cudaDeviceProp prop;
     if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, device);
@@ -68,15 +108,16 @@ extern "C" rt_status rt_context_create(int device, rt_context **out) {
         delete ctx;
         return RT_ERR_NO_DEVICE;
     }
-    // Library-owned bookkeeping: error word + work counters.
+    // Library-owned bookkeeping: error word + work counters + the bandwidth
+    // probe's sink word.
     void *p = nullptr;
-    if (cudaMalloc(&p, (2u + kNumCounters) * sizeof(uint32_t)) != cudaSuccess) {
+    if (cudaMalloc(&p, (3u + kNumCounters) * sizeof(uint32_t)) != cudaSuccess) {
         delete ctx;
         return RT_ERR_OOM;
     }
     ctx->d_err = static_cast<uint32_t *>(p);
     ctx->d_counters = ctx->d_err + 2;
-    if (cudaMemset(p, 0, (2u + kNumCounters) * sizeof(uint32_t)) != cudaSuccess) {
+    if (cudaMemset(p, 0, (3u + kNumCounters) * sizeof(uint32_t)) != cudaSuccess) {
         cudaFree(p);
         delete ctx;
         return RT_ERR_CUDA;

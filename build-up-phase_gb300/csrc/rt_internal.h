@@ -43,6 +43,10 @@ struct rt_context {
     int pageable_state = 0;      // 0 not queried, 1 pageable memory reachable in place, 2 not
     const void *host_scratch = nullptr;  // the ring the events above refer to
     uint64_t host_scratch_bytes = 0;
+    // Polls of a predecessor tile's status the onesweep look-back makes
+    // before it gives up with RT_ERR_TIMEOUT (rt_debug_set_sort_spin_limit).
+    static constexpr uint32_t kSortSpinLimit = 1u << 22;
+    uint32_t sort_spin_limit = kSortSpinLimit;
 };
 
 namespace rtc {
@@ -109,6 +113,11 @@ uint64_t sort_scratch_bytes(uint32_t n, int passes);
 int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
                uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err);
 uint32_t *sort_hist_ptr(void *scratch);
+
+// Forgets the cached device address of the allocation-free build's static
+// scratch array on `device` (rt_build.cu); rt_context_create calls it so that
+// a context made after a device reset looks the address up again.
+void static_scratch_forget(int device);
 
 }  // namespace rtc
 

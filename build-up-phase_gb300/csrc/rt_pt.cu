@@ -30,6 +30,7 @@
 
 #include "../../include/rtcore_batch.h"
 #include "../../include/rtcore_pt.h"
+#include "../../include/rtcore_debug.h"
 #include "rt_internal.h"
 #include "rt_pt_math.cuh"
 #include "rt_traverse.cuh"
@@ -918,6 +919,25 @@ extern "C" rt_status rt_path_trace_cached(rt_context *ctx, rt_stream stream, con
                                           void *scratch, uint64_t scratch_bytes) {
     if (!cp) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace_cached: null cache parameters");
     return path_trace_impl(ctx, stream, scene, p, cp, accum, scratch, scratch_bytes);
+}
+
+extern "C" rt_status rt_debug_pt_cache_layout(const rt_pt_params *p, const rt_pt_cache_params *cp, uint32_t n_lights,
+                                              rt_debug_pt_cache_offsets *out) {
+    if (!p || !cp || !out) return RT_ERR_INVALID_ARG;
+    const uint64_t npix = (uint64_t)p->width * p->height;
+    const PtLayout L = pt_layout(*p, n_lights, train_capacity(npix, cp->train_paths));
+    out->query_count = L.counters + (uint64_t)kCntQuery * 4u;
+    out->query_in = L.qin;
+    out->query_t1 = L.qt1;
+    out->query_path = L.qpidx;
+    out->query_out = L.qout;
+    out->train_count = L.counters + (uint64_t)kCntTrain * 4u;
+    out->train_in = L.tin;
+    out->train_t1 = L.tt1;
+    out->train_before = L.tlpre;
+    out->train_path = L.tpidx;
+    out->train_target = L.ttarget;
+    return RT_OK;
 }
 
 extern "C" rt_status rt_pt_ray_counts(rt_context *ctx, rt_stream stream, const rt_pt_params *p, uint32_t n_lights,

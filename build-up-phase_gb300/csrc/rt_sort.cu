@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "rt_internal.h"
+#include "../../include/rtcore_debug.h"
 
 namespace rtc {
 
@@ -31,7 +32,6 @@ constexpr int kRadix = 256;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagIncl = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-constexpr int kSpinLimit = 1 << 22;
 
 constexpr size_t kSortSmemBytes =
     (size_t)kSortTile * 8u + (size_t)kSortTile * 4u + (size_t)kSortWarps * kRadix * 4u;
@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
                                                             uint32_t *__restrict__ vout, uint32_t n, int shift, uint32_t dmask,
                                                             const uint32_t *__restrict__ hist,
                                                             uint32_t *__restrict__ status,
-                                                            uint32_t *__restrict__ tile_counter, uint32_t *err) {
+                                                            uint32_t *__restrict__ tile_counter, uint32_t *err,
+                                                            uint32_t spin_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + kSortTile);
@@ -168,10 +169,10 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
             int64_t p = (int64_t)tile - 1;
             while (p >= 0) {
                 uint32_t s;
-                int spins = 0;
+                uint32_t spins = 0;
                 do {
                     s = st[(size_t)p * kRadix + t];
-                } while ((s & ~kValueMask) == 0u && ++spins < kSpinLimit);
+                } while ((s & ~kValueMask) == 0u && ++spins < spin_limit);
                 if ((s & ~kValueMask) == 0u) {
                     report_error(err, RT_ERR_TIMEOUT, 0x50000000u | (uint32_t)tile);
                     break;
@@ -255,7 +256,8 @@ int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint
         uint64_t *ko = (p & 1) ? keys0 : keys1;
         uint32_t *vo = (p & 1) ? vals0 : vals1;
         k_onesweep<<<(unsigned)tiles, kSortThreads, kSortSmemBytes, stream>>>(
-            ki, vi, ko, vo, n, 8 * p, digit_mask(key_bits, p), hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err);
+            ki, vi, ko, vo, n, 8 * p, digit_mask(key_bits, p), hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err,
+            ctx->sort_spin_limit);
         RT_CUDA_TRY(cudaGetLastError());
     }
     if (passes & 1) {
@@ -276,6 +278,12 @@ extern "C" rt_status rt_get_sort_scratch_bytes(uint32_t n, uint32_t key_bits, ui
     if (!out || key_bits == 0 || key_bits > 64) return RT_ERR_INVALID_ARG;
     int passes = (int)((key_bits + 7u) / 8u);
     *out = rtc::align_up((uint64_t)n * 12u, 256) + rtc::sort_scratch_bytes(n, passes);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_debug_set_sort_spin_limit(rt_context *ctx, uint32_t spins) {
+    if (!ctx) return RT_ERR_INVALID_ARG;
+    ctx->sort_spin_limit = spins ? spins : rt_context::kSortSpinLimit;
     return RT_OK;
 }
 

@@ -21,9 +21,13 @@
 // siblings are pushed as one group.  Closest hit = smallest t, ties broken by
 // the smallest (instance, triangle) key.
 #include <cmath>
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include "rt_internal.h"
+#include "../../include/rtcore_debug.h"
 #include "rt_traverse.cuh"
 
 namespace rtc {
@@ -774,15 +778,57 @@ int host_setup(rt_context *ctx) {
     return RT_OK;
 }
 
+// Whether every page of the host range [p, p + bytes) is mapped in this
+// process.  msync with MS_ASYNC writes nothing back; it only fails with ENOMEM
+// where part of the range is unmapped (a gap between two allocations, which a
+// kernel reading the range in place would fault on).
+bool host_range_mapped(const void *p, uint64_t bytes) {
+    const long pg = sysconf(_SC_PAGESIZE);
+    const uintptr_t page = pg > 0 ? (uintptr_t)pg : 4096u;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(p) & ~(page - 1u);
+    const uintptr_t hi = (reinterpret_cast<uintptr_t>(p) + bytes + page - 1u) & ~(page - 1u);
+    return msync(reinterpret_cast<void *>(lo), hi - lo, MS_ASYNC) == 0;
+}
+
+// Whether [p, p + bytes) lies inside one CUDA allocation (device, managed or
+// pinned host memory), from the driver's pointer attributes; false where the
+// driver cannot say.
+bool one_cuda_allocation(const void *p, uint64_t bytes) {
+    static decltype(&cuPointerGetAttribute) get_attr = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            (void)cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<decltype(&cuPointerGetAttribute)>(f);
+    }();
+    if (!get_attr) return false;
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    const CUdeviceptr q = (CUdeviceptr)reinterpret_cast<uintptr_t>(p);
+    if (get_attr(&base, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, q) != CUDA_SUCCESS ||
+        get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, q) != CUDA_SUCCESS)
+        return false;
+    return q >= base && q - base + bytes <= size;
+}
+
 // True when kernels reach [p, p + bytes) at the same address: pinned or
 // registered host memory under unified addressing (cudaHostAlloc,
 // cudaHostRegister), device or managed memory, and -- where the device
 // accesses pageable memory through the host's page tables (a Grace system's
 // NVLink-C2C; `pageable` from the device attributes) -- plain pageable
-// memory.
+// memory.  Both ends are checked, and so is what lies between them: a host
+// range must be mapped throughout (and, without pageable access, be one
+// pinned allocation), a device range must be one allocation.  Anything else
+// goes through the staged copies.
 bool reachable_in_place(const void *p, uint64_t bytes, bool pageable) {
+    if (bytes == 0) return true;
     const uint8_t *b = static_cast<const uint8_t *>(p);
-    for (const uint8_t *q : {b, b + (bytes ? bytes - 1u : 0u)}) {
+    bool host_side = true, device_side = true;
+    for (const uint8_t *q : {b, b + (bytes - 1u)}) {
         cudaPointerAttributes at;
         if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
             (void)cudaGetLastError();
@@ -790,11 +836,19 @@ bool reachable_in_place(const void *p, uint64_t bytes, bool pageable) {
         }
         if (at.type == cudaMemoryTypeHost) {
             if (at.devicePointer != q) return false;
+            device_side = false;
         } else if (at.type == cudaMemoryTypeUnregistered) {
             if (!pageable) return false;
+            device_side = false;
+        } else {
+            host_side = false;
         }
     }
-    return true;
+    if (host_side) {
+        if (!host_range_mapped(p, bytes)) return false;
+        return pageable || one_cuda_allocation(p, bytes);
+    }
+    return device_side && one_cuda_allocation(p, bytes);
 }
 
 // Whether the context's device reads and writes pageable host memory
@@ -858,7 +912,10 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
         uint8_t *rays_d = S + (uint64_t)s * H.slot_bytes;
         uint8_t *out_d = rays_d + H.out_offset;
         RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->h2d, ctx->ev_free[s], 0));
-        RT_CUDA_CTX(ctx, cudaMemcpyAsync(rays_d, hrays + off, (size_t)m * 32u, cudaMemcpyHostToDevice, ctx->h2d));
+        // cudaMemcpyDefault: the direction follows from the pointers (unified
+        // addressing), so a device or managed buffer handed to the host API
+        // copies correctly too
+        RT_CUDA_CTX(ctx, cudaMemcpyAsync(rays_d, hrays + off, (size_t)m * 32u, cudaMemcpyDefault, ctx->h2d));
         RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_loaded[s], ctx->h2d));
         RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ts, ctx->ev_loaded[s], 0));
         rc = launch_batch(ctx, ts, accel, reinterpret_cast<const rt_ray *>(rays_d),
@@ -868,7 +925,7 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
         RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_traced[s], ts));
         RT_CUDA_CTX(ctx, cudaStreamWaitEvent(ctx->d2h, ctx->ev_traced[s], 0));
         RT_CUDA_CTX(ctx, cudaMemcpyAsync(static_cast<uint8_t *>(hout) + (size_t)off * out_size, out_d,
-                                         (size_t)m * out_size, cudaMemcpyDeviceToHost, ctx->d2h));
+                                         (size_t)m * out_size, cudaMemcpyDefault, ctx->d2h));
         RT_CUDA_CTX(ctx, cudaEventRecord(ctx->ev_free[s], ctx->d2h));
     }
     // the caller's stream goes on after the last results have left
@@ -877,6 +934,13 @@ int trace_host(rt_context *ctx, cudaStream_t st, uint64_t accel, const rt_ray *h
 }
 
 }  // namespace
+
+extern "C" rt_status rt_debug_host_in_place(rt_context *ctx, const void *p, uint64_t bytes, int *in_place) {
+    if (!ctx || !in_place || (bytes && !p)) return RT_ERR_INVALID_ARG;
+    RT_CUDA_CTX(ctx, cudaSetDevice(ctx->device));
+    *in_place = reachable_in_place(p, bytes, pageable_in_place(ctx)) ? 1 : 0;
+    return RT_OK;
+}
 
 extern "C" rt_status rt_set_host_transfer(rt_context *ctx, uint32_t mode) {
     if (!ctx) return RT_ERR_INVALID_ARG;

@@ -139,6 +139,13 @@ class PtCacheParams(C.Structure):
     _fields_ = [("cache", C.c_void_p), ("train_paths", C.c_uint32), ("train_batch", C.c_uint32)]
 
 
+class PtCacheLayout(C.Structure):
+    """rt_debug_pt_cache_layout: byte offsets of the learned form's arrays."""
+    _fields_ = [(f, C.c_uint64) for f in ("query_count", "query_in", "query_t1", "query_path", "query_out",
+                                          "train_count", "train_in", "train_t1", "train_before", "train_path",
+                                          "train_target")]
+
+
 class BatchScene(C.Structure):
     _fields_ = [("scene", PtScene), ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("accum", C.c_void_p)]
@@ -202,6 +209,11 @@ PROTOTYPES = {
     "rt_get_sort_scratch_bytes": (_i32, [_u32, _u32, C.POINTER(_u64)]),
     "rt_sort_pairs": (_i32, [_vp, _vp, _vp, _vp, _u32, _u32, _vp, _u64]),
     "rt_debug_blas_scratch_layout": (_i32, [_u32, _u32, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    "rt_debug_set_sort_spin_limit": (_i32, [_vp, _u32]),
+    "rt_debug_host_in_place": (_i32, [_vp, _vp, _u64, C.POINTER(_i32)]),
+    "rt_debug_read_sweep": (_i32, [_vp, _vp, _vp, _u64, _u32]),
+    "rt_debug_pt_cache_layout": (_i32, [C.POINTER(PtParams), C.POINTER(PtCacheParams), _u32,
+                                        C.POINTER(PtCacheLayout)]),
     # path tracer declared in include/rtcore_pt.h
     "rt_pt_scratch_bytes": (_i32, [C.POINTER(PtParams), C.POINTER(_u64)]),
     "rt_path_trace": (_i32, [_vp, _vp, C.POINTER(PtScene), C.POINTER(PtParams), _vp, _vp, _u64]),
@@ -531,6 +543,32 @@ class Context:
     def sort_pairs(self, keys, vals, n: int, key_bits: int, scratch, scratch_bytes: int, stream=None) -> None:
         self.check(self.lib.rt_sort_pairs(self.h, _stream_ptr(stream), _ptr(keys), _ptr(vals), n, key_bits,
                                           _ptr(scratch), scratch_bytes), "rt_sort_pairs")
+
+    def read_sweep(self, buf, nbytes: int, passes: int, stream=None) -> None:
+        """rt_debug_read_sweep: the bandwidth probe (reads buf `passes` times)."""
+        self.check(self.lib.rt_debug_read_sweep(self.h, _stream_ptr(stream), _ptr(buf), nbytes, passes),
+                   "rt_debug_read_sweep")
+
+    def host_in_place(self, ptr: int, nbytes: int) -> bool:
+        """rt_debug_host_in_place: would the host-memory ray API use
+        [ptr, ptr + nbytes) in place?"""
+        out = C.c_int()
+        self.check(self.lib.rt_debug_host_in_place(self.h, ptr, nbytes, C.byref(out)), "rt_debug_host_in_place")
+        return bool(out.value)
+
+    def set_sort_spin_limit(self, spins: int) -> None:
+        """rt_debug_set_sort_spin_limit (0 restores the default)."""
+        self.check(self.lib.rt_debug_set_sort_spin_limit(self.h, spins), "rt_debug_set_sort_spin_limit")
+
+    @staticmethod
+    def pt_cache_layout(params: PtParams, cp: PtCacheParams, n_lights: int) -> PtCacheLayout:
+        """rt_debug_pt_cache_layout: where the last wave's learned-form arrays
+        lie in the scratch of rt_path_trace_cached."""
+        out = PtCacheLayout()
+        rc = load().rt_debug_pt_cache_layout(C.byref(params), C.byref(cp), n_lights, C.byref(out))
+        if rc != RT_OK:
+            raise RtError(rc, "rt_debug_pt_cache_layout")
+        return out
 
 
 def _scene_array(scenes):

@@ -1,14 +1,20 @@
-"""Renders the box scene with the wavefront path tracer and reports its speed.
+"""Command-line renderer: the box workload (a closed, lit box of 12
+triangles with --spheres icospheres of 20 x --freq^2 triangles each) path
+traced with rt_path_trace, written as a PPM (8-bit) and/or PFM (lossless
+float) image, with its speed reported.
 
     python -m rtcore.pt [--spheres 40] [--freq 50] [--width 1920] [--height 1080]
                         [--spp 4] [--calls 1] [--depth 8] [--binning]
                         [--ppm out.ppm] [--pfm out.pfm]
 
 One warm-up call, then --calls timed calls of --spp samples each (CUDA events
-on the launching stream); prints one JSON line with the milliseconds per
-sample, the extension and shadow rays per sample and M rays/s.
---binning traces the bounce rays grouped by direction octant instead of in
-shading order (RT_PT_OCTANT_BINNING; the image is the same).
+on the launching stream); the image holds all (calls + 1) x spp samples of
+every pixel.  Prints one JSON line with the milliseconds per sample, the
+extension and shadow rays per sample and M rays/s.  --binning traces the
+bounce rays grouped by direction octant instead of in shading order
+(RT_PT_OCTANT_BINNING; the image is the same).  It extends the image dump
+of the sample's storage-buffer exercise (vulkan-raytracing-basic/README.md:223)
+to the path tracer.
 """
 from __future__ import annotations
 

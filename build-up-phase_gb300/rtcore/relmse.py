@@ -7,8 +7,10 @@ path tracer, both measured against a converged plain reference.
 relMSE = mean over pixels and channels of (I - R)^2 / (R^2 + 0.01).  Both
 forms run four samples per call (one wave of four samples of every pixel; the
 learned form queries the cache once per wave and trains after it on the
-wave's training paths); the time of a call is its CUDA-event duration
-(training included for the learned form), image read-backs are not timed.
+wave's training paths).  Each call is timed twice: its CUDA-event duration
+(training included for the learned form) and its wall time (a host clock
+from just before the call to the end of a synchronisation after it); image
+read-backs for the relMSE are outside both.
 The curve is sampled at sample counts growing by 1.25x and at the end of the
 budget; the time to a target relMSE is interpolated log-log between the two
 samples around the crossing.
@@ -90,7 +92,8 @@ def _checkpoints(n: int):
 def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, cached: bool,
         train_paths: int = 65536, train_batch: int = 16384, seed: int = 777, lr: float = 1e-3,
         spp_per_call: int = 1):
-    """[(elapsed_ms, samples, relmse)] within the time budget."""
+    """[(gpu_ms, wall_ms, samples, relmse)] until the GPU time reaches the
+    budget: cumulative CUDA-event and wall-clock times of the calls."""
     import torch
     st = torch.cuda.current_stream()
     accum = torch.zeros(w * h * 16, dtype=torch.uint8, device="cuda")
@@ -105,11 +108,13 @@ def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: f
     else:
         nb = ctx.pt_scratch_bytes(p)
     scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
-    curve, elapsed, s = [], 0.0, 0
+    curve, elapsed, wall, s = [], 0.0, 0.0, 0
     marks = set(_checkpoints(1 << 20))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
     while elapsed < budget_ms:
         p = params(w, h, spc, s, seed)
+        t0 = time.perf_counter()
         e0.record(st)
         if cached:
             ctx.path_trace_cached(box.scene, p, cp, accum, scratch, nb)
@@ -117,28 +122,51 @@ def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: f
             ctx.path_trace(box.scene, p, accum, scratch, nb)
         e1.record(st)
         e1.synchronize()
+        wall += (time.perf_counter() - t0) * 1e3
         elapsed += e0.elapsed_time(e1)
         s += spc
         if any(k in marks for k in range(s - spc + 1, s + 1)) or elapsed >= budget_ms:
-            curve.append((round(elapsed, 3), s, relmse(_image(accum), ref)))
+            curve.append((round(elapsed, 3), round(wall, 3), s, relmse(_image(accum), ref)))
     ctx.sync()
     return curve
 
 
-def time_to(curve, target: float):
-    """Elapsed time at which relMSE first reaches target, interpolated
-    log-log between the samples around the crossing (None if never)."""
+def time_to(curve, target: float, clock: str = "gpu"):
+    """Elapsed time (clock "gpu": CUDA events, "wall": host clock) at which
+    relMSE first reaches target, interpolated log-log between the samples
+    around the crossing (None if never)."""
+    col = 0 if clock == "gpu" else 1
     prev = None
-    for ms, s, r in curve:
+    for row in curve:
+        ms, r = row[col], row[3]
         if r <= target:
-            if prev is None or prev[2] <= r or prev[0] <= 0.0:
+            if prev is None or prev[1] <= r or prev[0] <= 0.0:
                 return ms
             lt0, lt1 = math.log(prev[0]), math.log(ms)
-            lr0, lr1 = math.log(prev[2]), math.log(r)
+            lr0, lr1 = math.log(prev[1]), math.log(r)
             f = (math.log(target) - lr0) / (lr1 - lr0)
             return round(math.exp(lt0 + f * (lt1 - lt0)), 3)
-        prev = (ms, s, r)
+        prev = (ms, r)
     return None
+
+
+def equal_time(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, target: float = 1e-3,
+               train_paths: int = 65536, train_batch: int = 16384, lr: float = 1e-3, spp_per_call: int = 4) -> dict:
+    """Both forms against the reference within the budget: their curves,
+    relMSE at the end of the budget, the time each takes to reach `target`
+    on both clocks and the learned form's share of the plain form's time."""
+    plain = run(ctx, box, w, h, ref, budget_ms, False, spp_per_call=spp_per_call)
+    cached = run(ctx, box, w, h, ref, budget_ms, True, train_paths=train_paths, train_batch=train_batch, lr=lr,
+                 spp_per_call=spp_per_call)
+    out = {"curve_columns": ["gpu_ms", "wall_ms", "spp", "relmse"], "plain": plain, "cached": cached,
+           "relmse_at_budget": {"plain": plain[-1][3], "cached": cached[-1][3],
+                                "plain_spp": plain[-1][2], "cached_spp": cached[-1][2]},
+           "target": target}
+    for clock in ("gpu", "wall"):
+        tp, tc = time_to(plain, target, clock), time_to(cached, target, clock)
+        out[f"time_to_target_{clock}_ms"] = {"plain": tp, "cached": tc,
+                                             "ratio_cached_over_plain": round(tc / tp, 3) if tp and tc else None}
+    return out
 
 
 def main(argv=None) -> int:
@@ -172,12 +200,12 @@ def main(argv=None) -> int:
            "train_paths": a.train_paths, "train_batch": a.train_batch, "lr": a.lr,
            "plain_spp_per_call": a.plain_spp_per_call, "cached_spp_per_call": a.cached_spp_per_call,
            "reference_wall_s": round(t_ref, 1), "budget_ms": a.budget_ms,
-           "plain": plain, "cached": cached,
-           "relmse_at_budget": {"plain": plain[-1][2], "cached": cached[-1][2]},
-           "time_to_target_ms": {"target": a.target, "plain": time_to(plain, a.target),
-                                 "cached": time_to(cached, a.target)}}
-    tp, tc = res["time_to_target_ms"]["plain"], res["time_to_target_ms"]["cached"]
-    res["time_ratio_cached_over_plain"] = round(tc / tp, 3) if tp and tc else None
+           "curve_columns": ["gpu_ms", "wall_ms", "spp", "relmse"], "plain": plain, "cached": cached,
+           "relmse_at_budget": {"plain": plain[-1][3], "cached": cached[-1][3]}}
+    for clock in ("gpu", "wall"):
+        tp, tc = time_to(plain, a.target, clock), time_to(cached, a.target, clock)
+        res[f"time_to_target_{clock}_ms"] = {"target": a.target, "plain": tp, "cached": tc,
+                                             "ratio_cached_over_plain": round(tc / tp, 3) if tp and tc else None}
     js = json.dumps(res)
     print(js)
     if a.out:

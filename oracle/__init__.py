@@ -65,6 +65,9 @@ def load() -> C.CDLL:
         "orc_hw_threads": (u32, []),
         "orc_path_trace": (i32, [vp, vp, vp, u32, vp, u32, vp, vp, u32]),
         "orc_sincos_q": (None, [f, vp, vp]),
+        "orc_path_trace_pixels": (i32, [vp, vp, vp, u32, vp, u32, vp, u32, vp, u32, vp, u32]),
+        "orc_scene_soup": (i32, [u64, u32, vp, vp]),
+        "orc_scene_incoherent_rays": (i32, [u64, u32, vp, vp, f, vp]),
     }
     for name, (res, args) in protos.items():
         fn = getattr(lib, name)
@@ -309,6 +312,53 @@ def path_trace(accel: np.ndarray, tri_material: np.ndarray, materials: np.ndarra
     if rc != 0:
         raise RuntimeError(f"orc_path_trace returned {rc}")
     return accum
+
+
+CACHE_INPUT_DTYPE = np.dtype([("pos", "<f4", 3), ("dir", "<f4", 3), ("normal", "<f4", 3), ("albedo", "<f4", 3)])
+# orc_path_record (88 bytes)
+PATH_RECORD_DTYPE = np.dtype([("kind", "<u4"), ("L", "<f4", 3), ("L_before", "<f4", 3), ("t1", "<f4", 3),
+                              ("rec", CACHE_INPUT_DTYPE)])
+
+
+def path_trace_pixels(accel: np.ndarray, tri_material: np.ndarray, materials: np.ndarray, lights: np.ndarray,
+                      camera, width: int, height: int, pixels, spp: int = 1, max_depth: int = 8, rr_depth: int = 3,
+                      seed: int = 0, eps: float = 1e-4, sample_offset: int = 0, train_stride: int = 0,
+                      threads: int = 0) -> np.ndarray:
+    """The paths of rt_path_trace (train_stride 0) or rt_path_trace_cached
+    (its training stride) for the listed pixels only: PATH_RECORD_DTYPE
+    [len(pixels), spp]."""
+    lib = load()
+    px = np.ascontiguousarray(pixels, np.uint32)
+    out = np.zeros((len(px), spp), PATH_RECORD_DTYPE)
+    tm = np.ascontiguousarray(tri_material, np.uint32)
+    mats = np.ascontiguousarray(materials)
+    lts = np.ascontiguousarray(lights)
+    p = _PtParams(_Camera((C.c_float * 3)(*camera[0]), camera[1]), width, height, spp, sample_offset, max_depth,
+                  rr_depth, seed, eps, 0)
+    rc = lib.orc_path_trace_pixels(accel.ctypes.data, tm.ctypes.data, mats.ctypes.data, len(mats),
+                                   lts.ctypes.data if len(lts) else None, len(lts), C.byref(p), train_stride,
+                                   px.ctypes.data, len(px), out.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_path_trace_pixels returned {rc}")
+    return out
+
+
+def scene_soup(seed: int, n_tris: int):
+    """The triangle soup of rt_scene_soup, generated by the oracle:
+    (vertices float32 [3n, 3], indices uint32 [n, 3])."""
+    v = np.empty((3 * n_tris, 3), np.float32)
+    i = np.empty((n_tris, 3), np.uint32)
+    load().orc_scene_soup(seed, n_tris, v.ctypes.data, i.ctypes.data)
+    return v, i
+
+
+def incoherent_rays(seed: int, n: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), tmax: float = 1e30) -> np.ndarray:
+    """The rays of rt_scene_incoherent_rays, generated by the oracle."""
+    rays = np.empty(n, RAY_DTYPE)
+    lo_a = np.asarray(lo, np.float32)
+    hi_a = np.asarray(hi, np.float32)
+    load().orc_scene_incoherent_rays(seed, n, lo_a.ctypes.data, hi_a.ctypes.data, tmax, rays.ctypes.data)
+    return rays
 
 
 def sincos_q(x: float):

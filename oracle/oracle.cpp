@@ -811,13 +811,12 @@ bool traverse(const void *accel, const rt_ray &ray, HitState &hs, bool any_hit, 
 }
 
 template <class F>
-void parallel_for(uint32_t n, uint32_t n_threads, F f) {
+void parallel_for(uint32_t n, uint32_t n_threads, F f, uint32_t chunk = 4096) {
     if (n_threads == 0) n_threads = std::max(1u, std::thread::hardware_concurrency());
     if (n_threads > n) n_threads = n ? n : 1;
     if (n_threads <= 1) { f(0u, n); return; }
     std::vector<std::thread> th;
     std::atomic<uint32_t> next{0};
-    const uint32_t chunk = 4096;
     for (uint32_t k = 0; k < n_threads; ++k)
         th.emplace_back([&]() {
             for (;;) {
@@ -1296,6 +1295,34 @@ Rng rng_for(uint64_t seed, uint32_t sample, uint32_t pixel) {
     return g;
 }
 
+/* PCG32 stream `seq` started from `seed` (the workload generators). */
+Rng seeded_rng(uint64_t seed, uint64_t seq) {
+    Rng g;
+    g.inc = (seq << 1u) | 1u;
+    g.state = 0;
+    g.next();
+    g.state += seed;
+    g.next();
+    return g;
+}
+
+float uni_in(Rng &g, float a, float b) { return a + (b - a) * g.uni(); }
+
+/* Uniform direction on the unit sphere: rejection sampling from the cube. */
+void sphere_dir(Rng &g, float d[3]) {
+    for (;;) {
+        float x = 2.0f * g.uni() - 1.0f, y = 2.0f * g.uni() - 1.0f, z = 2.0f * g.uni() - 1.0f;
+        float r2 = (x * x + y * y) + z * z;
+        if (r2 > 1e-6f && r2 <= 1.0f) {
+            float inv = 1.0f / std::sqrt(r2);
+            d[0] = x * inv;
+            d[1] = y * inv;
+            d[2] = z * inv;
+            return;
+        }
+    }
+}
+
 /* Taylor polynomials of sin (to x^9) and cos (to x^8), |x| <= pi/4. */
 float poly_sin(float x) {
     float x2 = x * x;
@@ -1325,149 +1352,221 @@ extern "C" void orc_sincos_q(float x, float *s, float *c) {
     *c = poly_cos(x);
 }
 
-extern "C" int orc_path_trace(const void *accel, const uint32_t *tri_material, const rt_material *materials,
-                              uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights,
-                              const rt_pt_params *p, float *accum, uint32_t n_threads) {
-    const float kInvPi = 0.318309886183790671538f, kPi4 = 0.785398163397448309616f;
-    AccelView av = view_of(accel);
-    if (av.h->kind != RT_ACCEL_KIND_BLAS) return RT_ERR_INVALID_ARG;
-    std::vector<LightInfo> li(n_lights);
-    std::vector<float> cdf(n_lights + 1);
+namespace {
+
+/* Everything a path needs that does not depend on the pixel: the scene, the
+ * light table (per-light normal and area, the area CDF in light order) and
+ * the camera's aspect factors. */
+struct PtSetup {
+    const void *accel;
+    AccelView av;
+    const uint32_t *tri_material;
+    const rt_material *materials;
+    uint32_t n_materials;
+    const rt_pt_light *lights;
+    uint32_t n_lights;
+    const rt_pt_params *p;
+    std::vector<LightInfo> li;
+    std::vector<float> cdf;
+    float total, ax, ay;
+};
+
+int pt_setup(PtSetup &c, const void *accel, const uint32_t *tri_material, const rt_material *materials,
+             uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights, const rt_pt_params *p) {
+    c.accel = accel;
+    c.av = view_of(accel);
+    if (c.av.h->kind != RT_ACCEL_KIND_BLAS) return RT_ERR_INVALID_ARG;
+    c.tri_material = tri_material;
+    c.materials = materials;
+    c.n_materials = n_materials;
+    c.lights = lights;
+    c.n_lights = n_lights;
+    c.p = p;
+    c.li.resize(n_lights);
+    c.cdf.resize(n_lights + 1);
     float acc = 0.0f;
     for (uint32_t k = 0; k < n_lights; ++k) {
         const rt_pt_light &l = lights[k];
-        float e1[3], e2[3], c[3];
+        float e1[3], e2[3], cr[3];
         for (int a = 0; a < 3; ++a) { e1[a] = l.v1[a] - l.v0[a]; e2[a] = l.v2[a] - l.v0[a]; }
-        cross(e1, e2, c);
-        float len = std::sqrt(dot(c, c));
+        cross(e1, e2, cr);
+        float len = std::sqrt(dot(cr, cr));
         float inv = len > 0.0f ? 1.0f / len : 0.0f;
-        for (int a = 0; a < 3; ++a) li[k].n[a] = c[a] * inv;
-        li[k].area = 0.5f * len;
-        acc = acc + li[k].area;
-        cdf[k] = acc;
+        for (int a = 0; a < 3; ++a) c.li[k].n[a] = cr[a] * inv;
+        c.li[k].area = 0.5f * len;
+        acc = acc + c.li[k].area;
+        c.cdf[k] = acc;
     }
-    cdf[n_lights] = acc;
-    const float total = acc;
+    c.cdf[n_lights] = acc;
+    c.total = acc;
     const float half = (p->camera.y_fov_degree * (float)(3.14159265358979323846 / 180.0)) * 0.5f;
-    const float ay = (float)std::tan((double)half);
-    const float ax = (ay * (float)p->width) / (float)p->height;
+    c.ay = (float)std::tan((double)half);
+    c.ax = (c.ay * (float)p->width) / (float)p->height;
+    return RT_OK;
+}
+
+/* Training pixels of a sample in the learned form: (pixel + offset) % stride
+ * == 0, the offset drawn per sample from the seed (rt_path_trace_cached). */
+uint32_t train_offset(uint64_t seed, uint32_t sample, uint32_t stride) {
+    return (uint32_t)(mix64(seed ^ (0x5851f42d4c957f2dull + sample)) % stride);
+}
+
+/* One path: sample `sample` of pixel `pix`.  Adds its radiance to L.  With
+ * stride > 0 the path follows the learned form (rec receives what the
+ * second vertex recorded; a query path stops there, before next-event
+ * estimation); otherwise it is the plain path tracer. */
+int pt_sample(const PtSetup &c, uint32_t pix, uint32_t sample, uint32_t stride, orc_path_record *rec,
+              float L[3]) {
+    const float kInvPi = 0.318309886183790671538f, kPi4 = 0.785398163397448309616f;
+    const rt_pt_params *p = c.p;
+    int status = 0;
+    const uint32_t x = pix % p->width, y = pix / p->width;
+    Rng g = rng_for(p->seed, sample, pix);
+    float jx = g.uni(), jy = g.uni();
+    float sx = (float)x + jx, sy = (float)y + jy;
+    float ndx = (sx / (float)p->width) * 2.0f - 1.0f, ndy = (sy / (float)p->height) * 2.0f - 1.0f;
+    float pp = ndx * c.ax, qq = ndy * c.ay;
+    rt_ray ray;
+    for (int a = 0; a < 3; ++a) ray.org[a] = p->camera.position[a];
+    ray.dir[0] = (pp * 1.0f + qq * 0.0f) + 0.0f;
+    ray.dir[1] = (pp * 0.0f + qq * -1.0f) + 0.0f;
+    ray.dir[2] = (pp * 0.0f + qq * 0.0f) + -1.0f;
+    ray.tmin = 0.0f;
+    ray.tmax = 1e30f;
+    float T[3] = {1.0f, 1.0f, 1.0f};
+    const uint32_t off = stride ? train_offset(p->seed, sample, stride) : 0u;
+    for (uint32_t depth = 0; depth < p->max_depth; ++depth) {
+        float u[6];
+        for (int k = 0; k < 6; ++k) u[k] = g.uni();
+        HitState hs;
+        traverse(c.accel, ray, hs, false, 0xffu, nullptr);
+        if (!hs.found) break;
+        const float *r = (const float *)(c.av.prims + (size_t)hs.rec * 48u);
+        const float *v0 = r, *v1 = r + 4, *v2 = r + 8;
+        float P[3], e1[3], e2[3], ng[3], n[3];
+        for (int a = 0; a < 3; ++a) {
+            P[a] = ray.org[a] + hs.t * ray.dir[a];
+            e1[a] = v1[a] - v0[a];
+            e2[a] = v2[a] - v0[a];
+        }
+        cross(e1, e2, ng);
+        float len = std::sqrt(dot(ng, ng));
+        if (!(len > 0.0f)) break;
+        for (int a = 0; a < 3; ++a) n[a] = ng[a] / len;
+        float cosd = dot(n, ray.dir);
+        uint32_t mi = c.tri_material[hs.tri];
+        if (mi >= c.n_materials) { status = RT_ERR_BOUNDS; mi = 0; }
+        const rt_material &m = c.materials[mi];
+        if (depth == 0 && cosd < 0.0f)
+            for (int a = 0; a < 3; ++a) L[a] = L[a] + T[a] * m.emission[a];
+        if (cosd > 0.0f)
+            for (int a = 0; a < 3; ++a) n[a] = -n[a];
+        if (!(m.albedo[0] > 0.0f || m.albedo[1] > 0.0f || m.albedo[2] > 0.0f)) break;
+        if (stride && depth == 1u) {
+            for (int a = 0; a < 3; ++a) {
+                rec->rec.pos[a] = P[a];
+                rec->rec.dir[a] = -ray.dir[a];
+                rec->rec.normal[a] = n[a];
+                rec->rec.albedo[a] = m.albedo[a];
+                rec->t1[a] = T[a];
+                rec->L_before[a] = L[a];
+            }
+            if ((pix + off) % stride != 0u) {
+                rec->kind = 1u;  /* ends in a cache query */
+                return status;
+            }
+            rec->kind = 2u;      /* training path: goes on as plain path tracing */
+        }
+        if (c.n_lights > 0) {
+            float target = u[0] * c.total;
+            uint32_t lo = 0, hi = c.n_lights - 1u;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (c.cdf[mid] > target) hi = mid; else lo = mid + 1u;
+            }
+            const rt_pt_light &Lt = c.lights[lo];
+            float su = std::sqrt(u[1]);
+            float b0 = 1.0f - su, b1 = u[2] * su, b2 = (1.0f - b0) - b1;
+            float lp[3], wi[3];
+            for (int a = 0; a < 3; ++a) {
+                lp[a] = (Lt.v0[a] * b0 + Lt.v1[a] * b1) + Lt.v2[a] * b2;
+                wi[a] = lp[a] - P[a];
+            }
+            float dist2 = dot(wi, wi);
+            float dist = std::sqrt(dist2);
+            if (dist > 0.0f) {
+                float wn[3];
+                for (int a = 0; a < 3; ++a) wn[a] = wi[a] / dist;
+                float cos_s = dot(n, wn), cos_l = -dot(c.li[lo].n, wn);
+                if (cos_s > 0.0f && cos_l > 0.0f) {
+                    float f = (((cos_s * cos_l) / dist2) * c.total) * kInvPi;
+                    rt_ray sr;
+                    float contrib[3];
+                    for (int a = 0; a < 3; ++a) {
+                        contrib[a] = ((T[a] * m.albedo[a]) * Lt.emission[a]) * f;
+                        sr.org[a] = P[a] + n[a] * p->ray_eps;
+                    }
+                    for (int a = 0; a < 3; ++a) sr.dir[a] = lp[a] - sr.org[a];
+                    sr.tmin = 0.0f;
+                    sr.tmax = 0.9999f;
+                    HitState sh;
+                    if (!traverse(c.accel, sr, sh, true, 0xffu, nullptr))
+                        for (int a = 0; a < 3; ++a) L[a] = L[a] + contrib[a];
+                }
+            }
+        }
+        if (depth >= p->rr_depth) {
+            float ps = std::fmax(std::fmax(T[0], T[1]), T[2]);
+            ps = ps < 0.95f ? ps : 0.95f;
+            if (!(u[5] < ps)) break;
+            for (int a = 0; a < 3; ++a) T[a] = T[a] / ps;
+        }
+        if (depth + 1u >= p->max_depth) break;
+        /* cosine-weighted direction: concentric disk lifted to the hemisphere */
+        float da = 2.0f * u[3] - 1.0f, db = 2.0f * u[4] - 1.0f, dx, dy;
+        if (da == 0.0f && db == 0.0f) {
+            dx = 0.0f; dy = 0.0f;
+        } else if (std::fabs(da) > std::fabs(db)) {
+            float phi = kPi4 * (db / da);
+            dx = da * poly_cos(phi); dy = da * poly_sin(phi);
+        } else {
+            float phi = kPi4 * (da / db);
+            dx = db * poly_sin(phi); dy = db * poly_cos(phi);
+        }
+        float zz = (1.0f - dx * dx) - dy * dy;
+        float dz = std::sqrt(zz > 0.0f ? zz : 0.0f);
+        float sign = std::copysign(1.0f, n[2]);
+        float oa = -1.0f / (sign + n[2]);
+        float ob = n[0] * n[1] * oa;
+        float t1[3] = {1.0f + sign * n[0] * n[0] * oa, sign * ob, -sign * n[0]};
+        float t2[3] = {ob, sign + n[1] * n[1] * oa, -n[1]};
+        for (int a = 0; a < 3; ++a) {
+            ray.dir[a] = (t1[a] * dx + t2[a] * dy) + n[a] * dz;
+            ray.org[a] = P[a] + n[a] * p->ray_eps;
+            T[a] = T[a] * m.albedo[a];
+        }
+        ray.tmin = 0.0f;
+        ray.tmax = 1e30f;
+    }
+    return status;
+}
+
+}  // namespace
+
+extern "C" int orc_path_trace(const void *accel, const uint32_t *tri_material, const rt_material *materials,
+                              uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights,
+                              const rt_pt_params *p, float *accum, uint32_t n_threads) {
+    PtSetup c;
+    int rc = pt_setup(c, accel, tri_material, materials, n_materials, lights, n_lights, p);
+    if (rc) return rc;
     std::atomic<int> status{0};
     const uint32_t npix = p->width * p->height;
     parallel_for(npix, n_threads, [&](uint32_t b, uint32_t e) {
         for (uint32_t pix = b; pix < e; ++pix) {
-            const uint32_t x = pix % p->width, y = pix / p->width;
             for (uint32_t s = 0; s < p->spp; ++s) {
-                Rng g = rng_for(p->seed, p->sample_offset + s, pix);
-                float jx = g.uni(), jy = g.uni();
-                float sx = (float)x + jx, sy = (float)y + jy;
-                float ndx = (sx / (float)p->width) * 2.0f - 1.0f, ndy = (sy / (float)p->height) * 2.0f - 1.0f;
-                float pp = ndx * ax, qq = ndy * ay;
-                rt_ray ray;
-                for (int a = 0; a < 3; ++a) ray.org[a] = p->camera.position[a];
-                ray.dir[0] = (pp * 1.0f + qq * 0.0f) + 0.0f;
-                ray.dir[1] = (pp * 0.0f + qq * -1.0f) + 0.0f;
-                ray.dir[2] = (pp * 0.0f + qq * 0.0f) + -1.0f;
-                ray.tmin = 0.0f;
-                ray.tmax = 1e30f;
-                float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
-                for (uint32_t depth = 0; depth < p->max_depth; ++depth) {
-                    float u[6];
-                    for (int k = 0; k < 6; ++k) u[k] = g.uni();
-                    HitState hs;
-                    traverse(accel, ray, hs, false, 0xffu, nullptr);
-                    if (!hs.found) break;
-                    const float *rec = (const float *)(av.prims + (size_t)hs.rec * 48u);
-                    const float *v0 = rec, *v1 = rec + 4, *v2 = rec + 8;
-                    float P[3], e1[3], e2[3], ng[3], n[3];
-                    for (int a = 0; a < 3; ++a) {
-                        P[a] = ray.org[a] + hs.t * ray.dir[a];
-                        e1[a] = v1[a] - v0[a];
-                        e2[a] = v2[a] - v0[a];
-                    }
-                    cross(e1, e2, ng);
-                    float len = std::sqrt(dot(ng, ng));
-                    if (!(len > 0.0f)) break;
-                    for (int a = 0; a < 3; ++a) n[a] = ng[a] / len;
-                    float cosd = dot(n, ray.dir);
-                    uint32_t mi = tri_material[hs.tri];
-                    if (mi >= n_materials) { status = RT_ERR_BOUNDS; mi = 0; }
-                    const rt_material &m = materials[mi];
-                    if (depth == 0 && cosd < 0.0f)
-                        for (int a = 0; a < 3; ++a) L[a] = L[a] + T[a] * m.emission[a];
-                    if (cosd > 0.0f)
-                        for (int a = 0; a < 3; ++a) n[a] = -n[a];
-                    if (!(m.albedo[0] > 0.0f || m.albedo[1] > 0.0f || m.albedo[2] > 0.0f)) break;
-                    if (n_lights > 0) {
-                        float target = u[0] * total;
-                        uint32_t lo = 0, hi = n_lights - 1u;
-                        while (lo < hi) {
-                            uint32_t mid = (lo + hi) >> 1;
-                            if (cdf[mid] > target) hi = mid; else lo = mid + 1u;
-                        }
-                        const rt_pt_light &Lt = lights[lo];
-                        float su = std::sqrt(u[1]);
-                        float b0 = 1.0f - su, b1 = u[2] * su, b2 = (1.0f - b0) - b1;
-                        float lp[3], wi[3];
-                        for (int a = 0; a < 3; ++a) {
-                            lp[a] = (Lt.v0[a] * b0 + Lt.v1[a] * b1) + Lt.v2[a] * b2;
-                            wi[a] = lp[a] - P[a];
-                        }
-                        float dist2 = dot(wi, wi);
-                        float dist = std::sqrt(dist2);
-                        if (dist > 0.0f) {
-                            float wn[3];
-                            for (int a = 0; a < 3; ++a) wn[a] = wi[a] / dist;
-                            float cos_s = dot(n, wn), cos_l = -dot(li[lo].n, wn);
-                            if (cos_s > 0.0f && cos_l > 0.0f) {
-                                float f = (((cos_s * cos_l) / dist2) * total) * kInvPi;
-                                rt_ray sr;
-                                float contrib[3];
-                                for (int a = 0; a < 3; ++a) {
-                                    contrib[a] = ((T[a] * m.albedo[a]) * Lt.emission[a]) * f;
-                                    sr.org[a] = P[a] + n[a] * p->ray_eps;
-                                }
-                                for (int a = 0; a < 3; ++a) sr.dir[a] = lp[a] - sr.org[a];
-                                sr.tmin = 0.0f;
-                                sr.tmax = 0.9999f;
-                                HitState sh;
-                                if (!traverse(accel, sr, sh, true, 0xffu, nullptr))
-                                    for (int a = 0; a < 3; ++a) L[a] = L[a] + contrib[a];
-                            }
-                        }
-                    }
-                    if (depth >= p->rr_depth) {
-                        float ps = std::fmax(std::fmax(T[0], T[1]), T[2]);
-                        ps = ps < 0.95f ? ps : 0.95f;
-                        if (!(u[5] < ps)) break;
-                        for (int a = 0; a < 3; ++a) T[a] = T[a] / ps;
-                    }
-                    if (depth + 1u >= p->max_depth) break;
-                    /* cosine-weighted direction: concentric disk lifted to the hemisphere */
-                    float da = 2.0f * u[3] - 1.0f, db = 2.0f * u[4] - 1.0f, dx, dy;
-                    if (da == 0.0f && db == 0.0f) {
-                        dx = 0.0f; dy = 0.0f;
-                    } else if (std::fabs(da) > std::fabs(db)) {
-                        float phi = kPi4 * (db / da);
-                        dx = da * poly_cos(phi); dy = da * poly_sin(phi);
-                    } else {
-                        float phi = kPi4 * (da / db);
-                        dx = db * poly_sin(phi); dy = db * poly_cos(phi);
-                    }
-                    float zz = (1.0f - dx * dx) - dy * dy;
-                    float dz = std::sqrt(zz > 0.0f ? zz : 0.0f);
-                    float sign = std::copysign(1.0f, n[2]);
-                    float oa = -1.0f / (sign + n[2]);
-                    float ob = n[0] * n[1] * oa;
-                    float t1[3] = {1.0f + sign * n[0] * n[0] * oa, sign * ob, -sign * n[0]};
-                    float t2[3] = {ob, sign + n[1] * n[1] * oa, -n[1]};
-                    for (int a = 0; a < 3; ++a) {
-                        ray.dir[a] = (t1[a] * dx + t2[a] * dy) + n[a] * dz;
-                        ray.org[a] = P[a] + n[a] * p->ray_eps;
-                        T[a] = T[a] * m.albedo[a];
-                    }
-                    ray.tmin = 0.0f;
-                    ray.tmax = 1e30f;
-                }
+                float L[3] = {0.0f, 0.0f, 0.0f};
+                int st = pt_sample(c, pix, p->sample_offset + s, 0u, nullptr, L);
+                if (st) status = st;
                 float *px = accum + (size_t)pix * 4u;
                 for (int a = 0; a < 3; ++a) px[a] = px[a] + L[a];
                 px[3] = px[3] + 1.0f;
@@ -1475,4 +1574,62 @@ extern "C" int orc_path_trace(const void *accel, const uint32_t *tri_material, c
         }
     });
     return status.load();
+}
+
+extern "C" int orc_path_trace_pixels(const void *accel, const uint32_t *tri_material, const rt_material *materials,
+                                     uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights,
+                                     const rt_pt_params *p, uint32_t train_stride, const uint32_t *pixels,
+                                     uint32_t n_pixels, orc_path_record *out, uint32_t n_threads) {
+    PtSetup c;
+    int rc = pt_setup(c, accel, tri_material, materials, n_materials, lights, n_lights, p);
+    if (rc) return rc;
+    const uint32_t npix = p->width * p->height;
+    for (uint32_t k = 0; k < n_pixels; ++k)
+        if (pixels[k] >= npix) return RT_ERR_INVALID_ARG;
+    std::atomic<int> status{0};
+    const uint32_t n = n_pixels * p->spp;
+    parallel_for(n, n_threads, [&](uint32_t b, uint32_t e) {
+        for (uint32_t i = b; i < e; ++i) {
+            const uint32_t k = i / p->spp, s = i % p->spp;
+            orc_path_record &r = out[i];
+            std::memset(&r, 0, sizeof(r));
+            int st = pt_sample(c, pixels[k], p->sample_offset + s, train_stride, &r, r.L);
+            if (st) status = st;
+        }
+    }, 8u);
+    return status.load();
+}
+
+extern "C" int orc_scene_soup(uint64_t seed, uint32_t n_tris, float *v, uint32_t *idx) {
+    Rng g = seeded_rng(mix64(seed), 1u);
+    for (uint32_t i = 0; i < n_tris; ++i) {
+        float c[3] = {g.uni(), g.uni(), g.uni()};
+        float d1[3], d2[3];
+        sphere_dir(g, d1);
+        sphere_dir(g, d2);
+        float l1 = uni_in(g, 0.001f, 0.02f), l2 = uni_in(g, 0.001f, 0.02f);
+        float *q = v + (size_t)i * 9u;
+        for (int a = 0; a < 3; ++a) {
+            float e1 = d1[a] * l1, e2 = d2[a] * l2;
+            float v0 = c[a] - (e1 + e2) / 3.0f;
+            q[a] = v0;
+            q[3 + a] = v0 + e1;
+            q[6 + a] = v0 + e2;
+        }
+        for (uint32_t k = 0; k < 3; ++k) idx[3u * i + k] = 3u * i + k;
+    }
+    return 0;
+}
+
+extern "C" int orc_scene_incoherent_rays(uint64_t seed, uint32_t n, const float lo[3], const float hi[3], float tmax,
+                                         rt_ray *rays) {
+    Rng g = seeded_rng(mix64(seed), 3u);
+    for (uint32_t i = 0; i < n; ++i) {
+        rt_ray &r = rays[i];
+        for (int a = 0; a < 3; ++a) r.org[a] = uni_in(g, lo[a], hi[a]);
+        sphere_dir(g, r.dir);
+        r.tmin = 0.0f;
+        r.tmax = tmax;
+    }
+    return 0;
 }

@@ -23,6 +23,7 @@
 #include "../include/rtcore.h"
 #include "../include/rtcore_accel.h"
 #include "../include/rtcore_pt.h"
+#include "../include/rtcore_cache.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -104,6 +105,36 @@ int orc_trace_rays(const rt_pipeline *p, const float *sbt_colors,
 int orc_path_trace(const void *accel, const uint32_t *tri_material, const rt_material *materials,
                    uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights, const rt_pt_params *p,
                    float *accum, uint32_t n_threads);
+
+/* What one path of orc_path_trace_pixels brought back (88 bytes).  kind:
+ * 0 the path never reached a second reflective vertex (or the plain form),
+ * 1 it ended there in a cache query, 2 it is a training path.  L: the
+ * path's radiance (for a query path: before the cache's contribution);
+ * L_before, t1, rec: radiance, throughput and the cache input (position,
+ * direction toward the first vertex, normal, albedo) at the second vertex. */
+typedef struct orc_path_record {
+    uint32_t kind;
+    float L[3];
+    float L_before[3];
+    float t1[3];
+    rt_cache_input rec;
+} orc_path_record;
+
+/* The same paths for a list of pixels only: out[k * spp + s] is sample
+ * sample_offset + s of pixels[k].  train_stride 0: the plain path tracer;
+ * otherwise the learned form of rt_path_trace_cached with that training
+ * stride (training pixels (pixel + offset) % stride == 0 per sample). */
+int orc_path_trace_pixels(const void *accel, const uint32_t *tri_material, const rt_material *materials,
+                          uint32_t n_materials, const rt_pt_light *lights, uint32_t n_lights, const rt_pt_params *p,
+                          uint32_t train_stride, const uint32_t *pixels, uint32_t n_pixels, orc_path_record *out,
+                          uint32_t n_threads);
+
+/* The seeded workload generators of rtcore_scene.h (rt_scene_soup,
+ * rt_scene_incoherent_rays) restated, so that a CPU-only run can make the
+ * same inputs without the product library. */
+int orc_scene_soup(uint64_t seed, uint32_t n_tris, float *v, uint32_t *idx);
+int orc_scene_incoherent_rays(uint64_t seed, uint32_t n, const float lo[3], const float hi[3], float tmax,
+                              rt_ray *rays);
 
 /* sin and cos of the oracle's polynomial, for tests of their accuracy. */
 void orc_sincos_q(float x, float *s, float *c);

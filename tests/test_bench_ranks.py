@@ -62,3 +62,33 @@ def test_reference_arm_other_ranks_exit_without_work():
     r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "3",
                         "--warmup", "3"], capture_output=True, text=True, timeout=120, env=env)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_loads_only_the_oracle():
+    """The reference arm makes its inputs with the oracle's generators and
+    times the oracle: the product library is never mapped into its process
+    (a small soup and frame here; the arm itself runs the full workload)."""
+    code = (
+        "import sys, json, types; sys.path.insert(0, %r); import bench\n"
+        "bench.N_TRIS, bench.W, bench.H = 20000, 64, 32\n"
+        "bench.run_reference(types.SimpleNamespace(gpus=1, steps=1, warmup=1))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'librtcore': 'librtcore' in maps, 'liboracle': 'liboracle' in maps,"
+        " 'rtcore_imported': 'rtcore' in sys.modules}))\n" % str(REPO))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    import json
+    lines = r.stdout.strip().splitlines()
+    line, probe = json.loads(lines[0]), json.loads(lines[-1])
+    assert line["impl"] == "reference" and line["config"]["rays_per_step"] == 2 * 64 * 32
+    assert probe == {"librtcore": False, "liboracle": True, "rtcore_imported": False}, probe
+
+
+def test_primary_rays_of_both_arms_are_equal():
+    """The GPU arm's numpy raygen and the oracle's give the same rays."""
+    sys.path.insert(0, str(REPO))
+    import bench
+    import oracle
+    a = bench.primary_rays_np()
+    b = oracle.primary_rays(bench.CAMERA, bench.W, bench.H, 0.0, 100.0)
+    assert a.tobytes() == b.tobytes()

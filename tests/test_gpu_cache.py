@@ -10,6 +10,11 @@ from helpers import dev, host
 
 pytestmark = pytest.mark.gpu
 
+# Tolerances against the float64 oracle (which rounds where the kernels
+# round to BF16): about twice the errors observed on a GB300 (printed).
+FWD_TOL = 1e-2    # max |y - y_oracle| / max |y_oracle|
+GRAD_TOL = 3e-2   # per layer: max |g - g_oracle| / max |g_oracle|
+
 INPUT_DTYPE = np.dtype([("pos", "<f4", 3), ("dir", "<f4", 3), ("normal", "<f4", 3), ("albedo", "<f4", 3)])
 
 
@@ -63,7 +68,9 @@ def test_forward_matches_oracle(ctx, cache):
     p = get_params(ctx, cache)
     yo = mlp.forward(p, x, (-1, -1, -1), (1, 1, 1))[:, :3]
     scale = np.abs(yo).max()
-    assert np.abs(y[:, :3] - yo).max() / scale < 1e-2
+    err = np.abs(y[:, :3] - yo).max() / scale
+    print(f"forward, 1,000 rows: max error / max output {err:.3e} (tolerance {FWD_TOL:g})")
+    assert err < FWD_TOL
     assert np.all(y[:, 3] == 0)
 
 
@@ -80,7 +87,9 @@ def test_forward_many_tiles_matches_oracle(ctx, cache):
     idx = np.r_[np.random.default_rng(0).choice(len(x) - 64, 2000, replace=False), np.arange(len(x) - 64, len(x))]
     p = get_params(ctx, cache)
     yo = mlp.forward(p, x[idx], (-1, -1, -1), (1, 1, 1))[:, :3]
-    assert np.abs(y[idx, :3] - yo).max() / np.abs(yo).max() < 1e-2
+    err = np.abs(y[idx, :3] - yo).max() / np.abs(yo).max()
+    print(f"forward, 100,003 rows: max error / max output {err:.3e} (tolerance {FWD_TOL:g})")
+    assert err < FWD_TOL
 
 
 def test_gradient_matches_oracle(ctx, cache):
@@ -95,14 +104,19 @@ def test_gradient_matches_oracle(ctx, cache):
     gg = host(g).view(np.float32).astype(np.float64)
     p = get_params(ctx, cache)
     go, loss = mlp.gradient(p, x, t, (-1, -1, -1), (1, 1, 1))
+    seen = []
     for L in range(6):
         wo, bo = mlp.W_OFF[L]
         a, b = gg[wo:bo], go[wo:bo]
         rel = np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
         cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
-        assert rel < 3e-2 and cos > 0.999, (L, rel, cos)
         ab, bb = gg[bo:bo + mlp.OUT[L]], go[bo:bo + mlp.OUT[L]]
-        assert np.abs(ab - bb).max() <= 3e-2 * max(np.abs(bb).max(), 1e-30), L
+        relb = np.abs(ab - bb).max() / max(np.abs(bb).max(), 1e-30)
+        seen.append((L, float(rel), cos, float(relb)))
+    print("gradient per layer (layer, weight error / max, cosine, bias error / max): "
+          + ", ".join(f"({L}, {r:.2e}, {c:.6f}, {rb:.2e})" for L, r, c, rb in seen) + f"; tolerance {GRAD_TOL:g}")
+    for L, rel, cos, relb in seen:
+        assert rel < GRAD_TOL and cos > 0.999 and relb <= GRAD_TOL, (L, rel, cos, relb)
     # padded inputs / outputs never receive gradient
     assert np.all(gg[mlp.W_OFF[0][0]:mlp.W_OFF[0][1]].reshape(64, 96)[:, 81:] == 0)
     assert np.all(gg[mlp.W_OFF[5][0]:mlp.W_OFF[5][1]].reshape(8, 64)[3:] == 0)

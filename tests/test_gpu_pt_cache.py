@@ -3,10 +3,11 @@ the plain path tracer: what the trained network gains.
 
 1. The same learned form with and without training: after some frames the
    trained cache's image is much closer to the converged reference.
-2. Equal time against the plain path tracer at 1920x1080 on the 2M-triangle
-   box scene: the learned form reaches a lower relMSE.  (At low resolution
-   the fixed training cost per frame dominates and the plain form wins; the
-   cache pays off at the resolution it is designed for.)
+2. The learned workload's criterion at 1920x1080 on the 8M-triangle box
+   scene (160 icospheres): the learned form reaches the relMSE the plain form
+   has after its whole time budget in at most half of that time.  (At low
+   resolution the fixed training cost per frame dominates and the plain form
+   wins; the cache pays off at the resolution it is designed for.)
 """
 from __future__ import annotations
 
@@ -59,15 +60,25 @@ def test_training_gains_over_untrained_cache(ctx, box, spc):
     assert r_t < 0.5 * r_u, (r_t, r_u)
 
 
-def test_equal_time_beats_plain(ctx, box):
-    """1920x1080, 65,536 training paths per frame in batches of 16,384 (the
-    learned form's configuration), 1.5 s of GPU time each."""
-    from rtcore.relmse import reference, run
+def test_learned_form_needs_at_most_half_the_time(ctx):
+    """1920x1080 on the learned workload's 8,000,014-triangle box, 65,536
+    training paths per sample in Adam batches of 16,384, four samples per
+    call for both forms, 3 s of GPU time each, against a 2,048-spp plain
+    reference.  The target is the relMSE the plain form reaches at the end
+    of its budget; the learned form must reach it in at most half the plain
+    form's time, on the CUDA-event clock and on the wall clock.  (Against a
+    2,048-spp reference both curves carry the same reference noise, which
+    cancels in this comparison.)"""
+    from rtcore.relmse import GpuBox, equal_time, reference, time_to
+    box8 = GpuBox(ctx, 160, 50)
     w, h = 1920, 1080
-    ref = reference(ctx, box, w, h, 512)
-    plain = run(ctx, box, w, h, ref, 1500.0, False)
-    cached = run(ctx, box, w, h, ref, 1500.0, True, train_paths=65536, train_batch=16384)
-    # same wall time (within one frame), lower error
-    assert abs(plain[-1][0] - cached[-1][0]) < 50.0
-    assert cached[-1][2] < 0.9 * plain[-1][2], (plain[-1], cached[-1])
-    assert cached[-1][1] > plain[-1][1]  # cheaper samples
+    ref = reference(ctx, box8, w, h, 2048)
+    res = equal_time(ctx, box8, w, h, ref, 3000.0, target=1.0, spp_per_call=4)
+    plain, cached = res["plain"], res["cached"]
+    target = plain[-1][3]
+    for clock in ("gpu", "wall"):
+        tp, tc = time_to(plain, target, clock), time_to(cached, target, clock)
+        print(f"{clock}: plain reaches relMSE {target:.3e} at {tp} ms, learned at {tc} ms "
+              f"(ratio {tc / tp if tc and tp else None})")
+        assert tc is not None and tc <= 0.5 * tp, (clock, tp, tc, plain[-1], cached[-1])
+    assert cached[-1][2] > plain[-1][2]  # cheaper samples

@@ -87,3 +87,58 @@ def test_progressive_accumulation_equals_one_call(orc, rtlib):
     assert one.tobytes() == two.tobytes()
     again = orc.path_trace(accel, tm, m, lights, S.BOX_CAMERA, 24, 16, 6, seed=3, threads=1)
     assert again.tobytes() == one.tobytes()
+
+
+def test_pixel_subset_paths_equal_the_full_image(orc, rtlib):
+    """orc_path_trace_pixels (the per-pixel paths the full-size GPU tests
+    compare against) sums to orc_path_trace's image bit for bit; in the
+    learned form, exactly the training pixels of each sample -- the residue
+    class (pixel + offset) % stride == 0 -- that reach a second reflective
+    vertex train, the other such pixels end in a query with the radiance they
+    had before it, and a training path's radiance is the plain path's."""
+    import rtcore.scenes as S
+    v, i, tm, m = S.box(S.SEED_BASE + 3, 3, 6)
+    lights = S.emissive_lights(v, i, tm, m)
+    ob, rc = orc.build_blas([(v, i, None)])
+    assert rc == 0
+    w, h, spp, seed = 64, 48, 3, 99
+    img = orc.path_trace(ob, tm, m, lights, S.BOX_CAMERA, w, h, spp, 8, 3, seed, 1e-4, sample_offset=5)
+    px = np.arange(w * h, dtype=np.uint32)
+    rec = orc.path_trace_pixels(ob, tm, m, lights, S.BOX_CAMERA, w, h, px, spp=spp, seed=seed, sample_offset=5)
+    acc = np.zeros((w * h, 3), np.float32)
+    for s in range(spp):
+        acc = acc + rec["L"][:, s]
+    assert acc.tobytes() == img.reshape(-1, 4)[:, :3].tobytes()
+    assert (rec["kind"] == 0).all()
+    stride = 7
+    lrn = orc.path_trace_pixels(ob, tm, m, lights, S.BOX_CAMERA, w, h, px, spp=spp, seed=seed, sample_offset=5,
+                                train_stride=stride)
+    assert (lrn["kind"] == 1).any() and (lrn["kind"] == 2).any()
+    for s in range(spp):
+        k = lrn["kind"][:, s]
+        reached = k > 0
+        # the offset is drawn per sample: that sample's training pixels form one residue class
+        classes = {int(p % stride) for p in np.nonzero(k == 2)[0]}
+        assert len(classes) == 1, classes
+        c = classes.pop()
+        assert ((px % stride == c) == (k == 2))[reached].all()
+        train = k == 2
+        assert lrn["L"][train, s].tobytes() == rec["L"][train, s].tobytes()
+        query = k == 1
+        assert lrn["L_before"][query, s].tobytes() == lrn["L"][query, s].tobytes()
+
+
+def test_oracle_generators_equal_the_library(orc, rtlib):
+    """The oracle's restatement of the seeded soup and incoherent-ray
+    generators writes the library's bytes at the benchmark's full sizes (1M
+    triangles, 1920x1080 rays), so a CPU-only run can make the benchmark's
+    inputs without loading the product library."""
+    import rtcore.scenes as S
+    seed = S.SEED_BASE + 2
+    v, i = S.soup(seed, 1_000_000)
+    vo, io = orc.scene_soup(seed, 1_000_000)
+    assert v.tobytes() == vo.tobytes() and i.tobytes() == io.tobytes()
+    for lo, hi, tmax in (((0, 0, 0), (1, 1, 1), 1e30), ((-0.99,) * 3, (0.99,) * 3, 1e30), ((0, 0, 0), (1, 2, 3), 5.0)):
+        r = S.incoherent_rays(seed, 1920 * 1080, lo, hi, tmax)
+        ro = orc.incoherent_rays(seed, 1920 * 1080, lo, hi, tmax)
+        assert r.tobytes() == ro.tobytes()
