@@ -20,14 +20,12 @@
 //             order by one thread each.  Node and record positions come from
 //             grid-wide prefix sums, so the output is deterministic and equal
 //             byte for byte to the CPU restatement of the same steps.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
 
 #include "rt_internal.h"
 
-namespace cg = cooperative_groups;
 
 namespace rtc {
 
@@ -535,6 +533,7 @@ struct CollapseArgs {
     uint32_t *blk;
     uint4 *nodes_out;
     rt_accel_header *hdr;
+    uint32_t *bar;  // grid barrier: arrival count, generation (zeroed before the launch)
     uint32_t *err;
 };
 
@@ -938,12 +937,48 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_red,
     return before + x - v;
 }
 
+// Grid-wide barrier of the cooperative collapse (its blocks are co-resident):
+// one arrival per block on a global counter, the last arrival opens the next
+// generation.  The wait is bounded: a block that gives up records
+// RT_ERR_TIMEOUT and returns false (the collapse then stops).
+constexpr uint32_t kCoopSpin = 1u << 22;
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ bool coop_sync(uint32_t *bar, uint32_t nblocks, uint32_t *err, uint32_t code) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const uint32_t gen = ld_acquire_u32(bar + 1);
+        __threadfence();
+        if (atomicAdd(bar, 1u) + 1u == nblocks) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            uint32_t it = 0;
+            while (ld_acquire_u32(bar + 1) == gen && ++it < kCoopSpin) {
+            }
+            if (it >= kCoopSpin) {
+                report_error(err, RT_ERR_TIMEOUT, code);
+                ok = 0;
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
-    cg::grid_group grid = cg::this_grid();
     __shared__ uint32_t s_red[kCollapseThreads / 32];
     const uint32_t G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
     if (b == 0 && t == 0) a.wq[0] = a.root_ref;
-    grid.sync();
+    if (!coop_sync(a.bar, G, a.err, 0x64000000u)) return;
     uint32_t level_start = 0, level_count = 1, prim_next = 0, depth = 0;
     // Every block evaluates the same level sizes, so all leave together; the
     // level cap (a wide tree is never deeper than its <= 96-level binary
@@ -972,7 +1007,7 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
         my_int = block_sum<kCollapseThreads>(my_int, s_red);
         my_prim = block_sum<kCollapseThreads>(my_prim, s_red);
         if (t == 0) { a.blk[2 * b] = my_int; a.blk[2 * b + 1] = my_prim; }
-        grid.sync();
+        if (!coop_sync(a.bar, G, a.err, 0x64000000u | depth)) return;
         uint32_t pre_i = 0, pre_p = 0, tot_i = 0, tot_p = 0;
         for (uint32_t q = t; q < G; q += kCollapseThreads) {
             uint32_t vi = __ldcg(a.blk + 2 * q), vp = __ldcg(a.blk + 2 * q + 1);
@@ -1001,7 +1036,7 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
         level_start = next_start;
         level_count = tot_i;
         prim_next += tot_p;
-        grid.sync();
+        if (!coop_sync(a.bar, G, a.err, 0x65000000u | depth)) return;
     }
     if (b == 0 && t == 0) {
         Box rb = ref_box(a, a.root_ref);
@@ -1168,7 +1203,9 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     ca.blk = reinterpret_cast<uint32_t *>(S + L.blk);
     ca.nodes_out = reinterpret_cast<uint4 *>(A + h.node_offset);
     ca.hdr = reinterpret_cast<rt_accel_header *>(A);
+    ca.bar = reinterpret_cast<uint32_t *>(S + L.misc + 128u);
     ca.err = ctx->d_err;
+    RT_CUDA_CTX(ctx, cudaMemsetAsync(ca.bar, 0, 2u * sizeof(uint32_t), st));
     int G = coop_grid(ctx);
     if (G <= 0) return set_error(ctx, RT_ERR_CUDA, "cooperative occupancy query failed");
     // Small levels gain nothing from a huge grid; fewer blocks make each

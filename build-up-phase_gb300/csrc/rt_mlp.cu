@@ -200,19 +200,49 @@ __device__ __forceinline__ void ldsm_x2_t(const void *p, uint32_t &r0, uint32_t 
 }
 
 // Weights (BF16, padded rows; the 8-output layer padded to 16 zero rows) and
-// FP32 biases into shared memory, 16 bytes at a time.
+// FP32 biases into shared memory, 16 bytes at a time.  Every thread issues
+// all of its loads before it stores any (the chunks are independent), so the
+// copy costs about one memory round trip instead of one per layer and step:
+// 5.5 us of a 16,384-sample batch when each layer's loads waited on the
+// previous layer's stores.
+constexpr int kTrainWChunks = 64 * 12 + 4 * 64 * 8 + 16 * 8;  // 2,944 sixteen-byte chunks
+constexpr int kTrainWPerThread = (kTrainWChunks + kTrainThreads - 1) / kTrainThreads;
+__device__ __forceinline__ void train_chunk(int e, int &l, int &o, int &c) {
+    if (e < 768) { l = 0; o = e / 12; c = e % 12; }
+    else if (e < 2816) { l = 1 + (e - 768) / 512; o = ((e - 768) % 512) / 8; c = (e - 768) % 8; }
+    else { l = 5; o = (e - 2816) / 8; c = (e - 2816) % 8; }
+}
 __device__ void load_weights_train(const CacheState *S, __nv_bfloat16 *sW, float *sB) {
-    for (int l = 0; l < kLayers; ++l) {
-        const int in = in_dim(l), chunks = in / 8;
-        const uint4 *gw = reinterpret_cast<const uint4 *>(S->wbf + w_off(l));
-        for (int e = threadIdx.x; e < tw_rows(l) * chunks; e += blockDim.x) {
-            const int o = e / chunks, c = e % chunks;
-            const uint4 v = o < out_dim(l) ? gw[o * chunks + c] : make_uint4(0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4 *>(sW + tw_off(l) + o * w_stride(l) + 8 * c) = v;
+    uint4 r[kTrainWPerThread];
+#pragma unroll
+    for (int k = 0; k < kTrainWPerThread; ++k) {
+        const int e = threadIdx.x + k * kTrainThreads;
+        r[k] = make_uint4(0u, 0u, 0u, 0u);
+        if (e < kTrainWChunks) {
+            int l, o, c;
+            train_chunk(e, l, o, c);
+            if (o < out_dim(l)) r[k] = reinterpret_cast<const uint4 *>(S->wbf + w_off(l))[o * (in_dim(l) / 8) + c];
         }
     }
-    for (int l = 0; l < kLayers; ++l)
-        for (int e = threadIdx.x; e < out_dim(l); e += blockDim.x) sB[(l < 5 ? 64 * l : 320) + e] = S->params[b_off(l) + e];
+    float b[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int e = threadIdx.x + k * kTrainThreads, l = e < 320 ? e / 64 : 5, o = e < 320 ? e % 64 : e - 320;
+        b[k] = (e < kBiasFloats && o < out_dim(l)) ? S->params[b_off(l) + o] : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < kTrainWPerThread; ++k) {
+        const int e = threadIdx.x + k * kTrainThreads;
+        if (e >= kTrainWChunks) continue;
+        int l, o, c;
+        train_chunk(e, l, o, c);
+        *reinterpret_cast<uint4 *>(sW + tw_off(l) + o * w_stride(l) + 8 * c) = r[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int e = threadIdx.x + k * kTrainThreads;
+        if (e < kBiasFloats) sB[e] = b[k];  // layer l's bias at 64 l, the output layer's at 320
+    }
 }
 
 // c[j] = A (16 x 16*KS, registers) * W (row-major [16*KS][*], shared memory,
@@ -280,7 +310,8 @@ __device__ __forceinline__ void warp_grad_w(const __nv_bfloat16 *sD, const __nv_
     }
 }
 
-// db[o] += sum_r delta[r][o] (threads o < OUT).
+// db[o] += sum_r delta[r][o] (threads o < OUT: the other warps meanwhile
+// run their weight-gradient MMAs).
 template <int OUT>
 __device__ __forceinline__ void grad_b(const __nv_bfloat16 *sD, float *gb) {
     const int t = threadIdx.x;
@@ -306,10 +337,13 @@ __device__ __forceinline__ void grads_of_layer(int L, const __nv_bfloat16 *sD, c
     }
 }
 
+// bump_step: this launch is followed by an Adam step (k_cache_adam), whose
+// step count it advances first (block 0), so no launch of its own is needed.
 __global__ void __launch_bounds__(kTrainThreads, 1) k_cache_fwd_bwd(CacheState *S, const rt_cache_input *in,
                                                                     const float4 *targets, uint32_t n,
                                                                     float inv_count, const uint32_t *n_dev,
-                                                                    uint32_t row0) {
+                                                                    uint32_t row0, uint32_t bump_step) {
+    if (bump_step && blockIdx.x == 0 && threadIdx.x == 0) S->step += 1u;
     if (n_dev) {
         // rows [row0, row0 + n) of a set whose size is produced on the device
         const uint32_t total = *n_dev;
@@ -741,10 +775,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cache_query_tc(const CacheSta
                      : "memory");
 }
 
-__global__ void k_cache_adam(CacheState *S) {
+// One Adam step on every parameter; S->step already counts it (advanced by
+// the k_cache_fwd_bwd launch before).  Thread 0 also hands the batch's mean
+// loss to loss_out and clears it for the next batch.
+__global__ void k_cache_adam(CacheState *S, float *loss_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        if (loss_out) *loss_out = S->loss;
+        S->loss = 0.0f;
+    }
     if (i >= kParams) return;
-    const uint32_t t = S->step + 1u;
+    const uint32_t t = S->step;
     const float g = S->grads[i];
     const float m = S->beta1 * S->m[i] + (1.0f - S->beta1) * g;
     const float v = S->beta2 * S->v[i] + (1.0f - S->beta2) * g * g;
@@ -756,14 +797,6 @@ __global__ void k_cache_adam(CacheState *S) {
     S->params[i] = p;
     S->wbf[i] = __float2bfloat16(p);
     S->grads[i] = 0.0f;
-}
-
-__global__ void k_cache_step(CacheState *S, float *loss_out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        S->step += 1u;
-        if (loss_out) *loss_out = S->loss;
-        S->loss = 0.0f;
-    }
 }
 
 __global__ void k_cache_refresh_bf16(CacheState *S) {
@@ -778,13 +811,13 @@ int set_smem(rt_context *ctx) {
 }
 
 int launch_fwd_bwd(rt_context *ctx, cudaStream_t st, CacheState *S, const rt_cache_input *in, const float *tg,
-                   uint32_t n) {
+                   uint32_t n, uint32_t bump_step) {
     const uint32_t tiles = (n + kTrainRows - 1) / kTrainRows;
     uint32_t grid = (uint32_t)ctx->sm_count;
     if (grid > tiles) grid = tiles;
     if (grid == 0) return RT_OK;
     k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(tg), n,
-                                                   1.0f / (3.0f * (float)n), nullptr, 0u);
+                                                   1.0f / (3.0f * (float)n), nullptr, 0u, bump_step);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }
@@ -876,10 +909,9 @@ extern "C" rt_status rt_cache_train(rt_context *ctx, rt_stream stream, void *cac
     CacheState *S = static_cast<CacheState *>(cache);
     for (uint32_t b = 0; b < n; b += batch) {
         const uint32_t m = (n - b) < batch ? (n - b) : batch;
-        rc = launch_fwd_bwd(ctx, st, S, in + b, targets + 4u * (size_t)b, m);
+        rc = launch_fwd_bwd(ctx, st, S, in + b, targets + 4u * (size_t)b, m, 1u);
         if (rc) return rc;
-        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S);
-        k_cache_step<<<1, 32, 0, st>>>(S, loss_out);
+        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S, loss_out);
         RT_CUDA_CTX(ctx, cudaGetLastError());
     }
     return RT_OK;
@@ -894,7 +926,7 @@ extern "C" rt_status rt_cache_gradient(rt_context *ctx, rt_stream stream, void *
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CacheState *S = static_cast<CacheState *>(cache);
     RT_CUDA_CTX(ctx, cudaMemsetAsync(S->grads, 0, sizeof(float) * kParams, st));
-    rc = launch_fwd_bwd(ctx, st, S, in, targets, n);
+    rc = launch_fwd_bwd(ctx, st, S, in, targets, n, 0u);
     if (rc) return rc;
     RT_CUDA_CTX(ctx, cudaMemcpyAsync(grad_out, S->grads, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
     RT_CUDA_CTX(ctx, cudaMemsetAsync(S->grads, 0, sizeof(float) * kParams, st));
@@ -1029,9 +1061,8 @@ int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cach
         uint32_t grid = (uint32_t)ctx->sm_count;
         if (grid > tiles) grid = tiles;
         k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(targets), m, 0.0f,
-                                                       n_dev, b);
-        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S);
-        k_cache_step<<<1, 32, 0, st>>>(S, nullptr);
+                                                       n_dev, b, 1u);
+        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S, nullptr);
         RT_CUDA_CTX(ctx, cudaGetLastError());
     }
     return RT_OK;

@@ -28,6 +28,16 @@ from . import Camera, Context, GeometryTriangles, PtCacheParams, PtParams, PtSce
 from . import scenes as S
 
 
+# Adam batch of the learned form's online training.  Smaller batches mean more
+# optimiser steps per frame for the same 65,536 samples, and on the GB300 the
+# steps are cheap next to the path tracing: on the 8M-triangle box at
+# 1920x1080 (four samples per call) the learned form reached the relMSE the
+# plain form has after 3 s of GPU time in 611 ms with batches of 4,096,
+# 759 ms with 8,192, 1,189 ms with 16,384, and it reached relMSE 1e-3 (against
+# 16,384 spp) in 2,579 / 4,095 / 6,623 ms with 16,384 / 32,768 / 65,536.
+TRAIN_BATCH = 4096
+
+
 def relmse(img: np.ndarray, ref: np.ndarray) -> float:
     return float(np.mean((img - ref) ** 2 / (ref * ref + 0.01)))
 
@@ -90,7 +100,7 @@ def _checkpoints(n: int):
 
 
 def run(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, cached: bool,
-        train_paths: int = 65536, train_batch: int = 16384, seed: int = 777, lr: float = 1e-3,
+        train_paths: int = 65536, train_batch: int = TRAIN_BATCH, seed: int = 777, lr: float = 1e-3,
         spp_per_call: int = 1):
     """[(gpu_ms, wall_ms, samples, relmse)] until the GPU time reaches the
     budget: cumulative CUDA-event and wall-clock times of the calls."""
@@ -151,7 +161,7 @@ def time_to(curve, target: float, clock: str = "gpu"):
 
 
 def equal_time(ctx: Context, box: GpuBox, w: int, h: int, ref: np.ndarray, budget_ms: float, target: float = 1e-3,
-               train_paths: int = 65536, train_batch: int = 16384, lr: float = 1e-3, spp_per_call: int = 4) -> dict:
+               train_paths: int = 65536, train_batch: int = TRAIN_BATCH, lr: float = 1e-3, spp_per_call: int = 4) -> dict:
     """Both forms against the reference within the budget: their curves,
     relMSE at the end of the budget, the time each takes to reach `target`
     on both clocks and the learned form's share of the plain form's time."""
@@ -180,7 +190,7 @@ def main(argv=None) -> int:
     ap.add_argument("--target", type=float, default=1e-3)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--train-paths", type=int, default=65536, help="training paths per frame")
-    ap.add_argument("--train-batch", type=int, default=16384)
+    ap.add_argument("--train-batch", type=int, default=TRAIN_BATCH)
     ap.add_argument("--plain-spp-per-call", type=int, default=4,
                     help="samples per call of the plain form (4: one wave of four samples)")
     ap.add_argument("--cached-spp-per-call", type=int, default=4,

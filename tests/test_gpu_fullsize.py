@@ -11,7 +11,7 @@ build of the same input.
     one wave of four samples per pixel, depth 8, Russian roulette from 3;
   * learned workload: the box with 160 icospheres (8,000,014 triangles),
     1920x1080, plain and learned forms (65,536 training paths per sample, Adam
-    batches of 16,384); for the learned form the cache query inputs recorded
+    batches of 4,096); for the learned form the cache query inputs recorded
     at the second vertex (x, -d, n, albedo), the throughput there, the
     training records and targets, and the image after the cache's answers
     are applied;
@@ -130,7 +130,7 @@ def test_box_8M_learned_form(ctx, orc, box8m):
     npix = W * H
     cache = torch.zeros(ctx.cache_bytes(), dtype=torch.uint8, device="cuda")
     ctx.cache_init(cache, rtcore.cache_config(seed=3))
-    cp = rtcore.PtCacheParams(cache.data_ptr(), 65536, 16384)
+    cp = rtcore.PtCacheParams(cache.data_ptr(), 65536, 4096)
     p0, p1 = box.params(4, 0), box.params(4, 4)
     nb = ctx.pt_cached_scratch_bytes(p1, cp)
     scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")

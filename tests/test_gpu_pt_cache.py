@@ -62,7 +62,7 @@ def test_training_gains_over_untrained_cache(ctx, box, spc):
 
 def test_learned_form_needs_at_most_half_the_time(ctx):
     """1920x1080 on the learned workload's 8,000,014-triangle box, 65,536
-    training paths per sample in Adam batches of 16,384, four samples per
+    training paths per sample in Adam batches of 4,096, four samples per
     call for both forms, 3 s of GPU time each, against a 2,048-spp plain
     reference.  The target is the relMSE the plain form reaches at the end
     of its budget; the learned form must reach it in at most half the plain
