@@ -273,7 +273,7 @@ __device__ __forceinline__ void warp_dense_wt(const uint32_t (&a)[KS][4], const 
 // cores; rows o >= OUT (padding) are dropped.
 template <int IN, int OUT, int NT>
 __device__ __forceinline__ void warp_grad_w(const __nv_bfloat16 *sD, const __nv_bfloat16 *sA, int as, int o0, int i0,
-                                            float *gW, int lane) {
+                                            float *gW, float *gb, int lane) {
     const int row = lane & 7, mat = lane >> 3, g = lane >> 2, q = lane & 3;
     float c[NT][4];
 #pragma unroll
@@ -299,41 +299,44 @@ __device__ __forceinline__ void warp_grad_w(const __nv_bfloat16 *sD, const __nv_
             }
         }
     }
+    // input IN is the tile's column of ones: its sums are the bias gradient;
+    // columns past it are discarded
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
         const int i = i0 + 8 * j + 2 * q;
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const int o = o0 + g + (e >= 2 ? 8 : 0);
-            if (o < OUT && c[j][e] != 0.0f) atomicAdd(gW + o * IN + i + (e & 1), c[j][e]);
+            const int o = o0 + g + (e >= 2 ? 8 : 0), ii = i + (e & 1);
+            if (o >= OUT || c[j][e] == 0.0f) continue;
+            if (ii < IN) atomicAdd(gW + o * IN + ii, c[j][e]);
+            else if (ii == IN) atomicAdd(gb + o, c[j][e]);
         }
     }
 }
 
-// db[o] += sum_r delta[r][o] (threads o < OUT: the other warps meanwhile
-// run their weight-gradient MMAs).
-template <int OUT>
-__device__ __forceinline__ void grad_b(const __nv_bfloat16 *sD, float *gb) {
-    const int t = threadIdx.x;
-    if (t < OUT) {
-        float s = 0.0f;
-        for (int r = 0; r < kTrainRows; ++r) s += __bfloat162float(sD[r * kDStride + t]);
-        if (s != 0.0f) atomicAdd(gb + t, s);
-    }
-}
-
-// The weight and bias gradients of layer L, split over the eight warps.
+// The weight and bias gradients of layer L, split over the eight warps.  The
+// input tiles carry a column of ones right after their last input (column 96
+// of the encoded inputs, 64 of the activations, in the row padding), so the
+// warps whose input range reaches it take one more n-tile and the MMAs leave
+// the bias gradient sum_r delta[r][o] there: no separate row loop (it held two
+// warps for ~2 us per layer while the block waited at its barrier).
 __device__ __forceinline__ void grads_of_layer(int L, const __nv_bfloat16 *sD, const __nv_bfloat16 *ain, int as,
                                                float *grads, int warp, int lane) {
     if (L == 0) {
-        warp_grad_w<96, 64, 6>(sD, ain, as, 16 * (warp & 3), 48 * (warp >> 2), grads + w_off(0), lane);
-        grad_b<64>(sD, grads + b_off(0));
+        if (warp >> 2)
+            warp_grad_w<96, 64, 8>(sD, ain, as, 16 * (warp & 3), 48, grads + w_off(0), grads + b_off(0), lane);
+        else
+            warp_grad_w<96, 64, 6>(sD, ain, as, 16 * (warp & 3), 0, grads + w_off(0), grads + b_off(0), lane);
     } else if (L == 5) {
-        warp_grad_w<64, 8, 1>(sD, ain, as, 0, 8 * warp, grads + w_off(5), lane);
-        grad_b<8>(sD, grads + b_off(5));
+        if (warp == 7)
+            warp_grad_w<64, 8, 2>(sD, ain, as, 0, 56, grads + w_off(5), grads + b_off(5), lane);
+        else
+            warp_grad_w<64, 8, 1>(sD, ain, as, 0, 8 * warp, grads + w_off(5), grads + b_off(5), lane);
     } else {
-        warp_grad_w<64, 64, 4>(sD, ain, as, 16 * (warp & 3), 32 * (warp >> 2), grads + w_off(L), lane);
-        grad_b<64>(sD, grads + b_off(L));
+        if (warp >> 2)
+            warp_grad_w<64, 64, 6>(sD, ain, as, 16 * (warp & 3), 32, grads + w_off(L), grads + b_off(L), lane);
+        else
+            warp_grad_w<64, 64, 4>(sD, ain, as, 16 * (warp & 3), 0, grads + w_off(L), grads + b_off(L), lane);
     }
 }
 
@@ -360,6 +363,15 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_cache_fwd_bwd(CacheState *
     __nv_bfloat16 *sAct = sIn + kTrainRows * kInStride;
     __nv_bfloat16 *sD = sAct + 5 * kTrainRows * kActStride;
     load_weights_train(S, sW, sB);
+    {
+        // the ones columns of the bias gradients (row padding, never written otherwise)
+        const uint4 ones = make_uint4(0x3f803f80u, 0x3f803f80u, 0x3f803f80u, 0x3f803f80u);
+        for (int e = threadIdx.x; e < 6 * kTrainRows; e += kTrainThreads) {
+            const int t = e / kTrainRows, r = e % kTrainRows;
+            if (t == 0) *reinterpret_cast<uint4 *>(sIn + r * kInStride + 96) = ones;
+            else *reinterpret_cast<uint4 *>(sAct + (t - 1) * kTrainRows * kActStride + r * kActStride + 64) = ones;
+        }
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, q = lane & 3;
     const int r0 = warp * 16;
