@@ -26,7 +26,10 @@ namespace {
 
 constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 8;
+// 16 keys per thread: tiles of 8,192 keys, half as many tiles for the
+// look-back's wave to cross (one 112 KB block per SM; 1M-key soup build
+// 0.807 -> 0.792 ms against 8 keys per thread, same bytes)
+constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 constexpr uint32_t kFlagAgg = 1u << 30;
