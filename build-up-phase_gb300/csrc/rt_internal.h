@@ -47,6 +47,7 @@ struct rt_context {
     // before it gives up with RT_ERR_TIMEOUT (rt_debug_set_sort_spin_limit).
     static constexpr uint32_t kSortSpinLimit = 1u << 22;
     uint32_t sort_spin_limit = kSortSpinLimit;
+    uint32_t sort_withhold = 0;  // rt_debug_set_sort_withhold
 };
 
 namespace rtc {
@@ -111,7 +112,8 @@ int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cach
 // Sort (rt_sort.cu)
 uint64_t sort_scratch_bytes(uint32_t n, int passes);
 int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
-               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err);
+               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err,
+               uint32_t withhold = 0u);
 uint32_t *sort_hist_ptr(void *scratch);
 
 // Forgets the cached device address of the allocation-free build's static

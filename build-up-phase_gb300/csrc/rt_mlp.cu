@@ -302,14 +302,18 @@ __device__ __forceinline__ void warp_grad_w(const __nv_bfloat16 *sD, const __nv_
     // input IN is the tile's column of ones: its sums are the bias gradient;
     // columns past it are discarded
 #pragma unroll
+    // (each lane holds two adjacent inputs of a row: one 8-byte vector add)
     for (int j = 0; j < NT; ++j) {
-        const int i = i0 + 8 * j + 2 * q;
+        const int i = i0 + 8 * j + 2 * q;  // even; IN is even
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int o = o0 + g + (e >= 2 ? 8 : 0), ii = i + (e & 1);
-            if (o >= OUT || c[j][e] == 0.0f) continue;
-            if (ii < IN) atomicAdd(gW + o * IN + ii, c[j][e]);
-            else if (ii == IN) atomicAdd(gb + o, c[j][e]);
+        for (int h = 0; h < 2; ++h) {
+            const int o = o0 + g + 8 * h;
+            const float x = c[j][2 * h], y = c[j][2 * h + 1];
+            if (o >= OUT || (x == 0.0f && y == 0.0f)) continue;
+            if (i < IN)
+                asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(gW + o * IN + i), "f"(x), "f"(y) : "memory");
+            else if (i == IN && x != 0.0f)
+                atomicAdd(gb + o, x);
         }
     }
 }
@@ -875,6 +879,7 @@ extern "C" uint32_t rt_cache_param_count(void) { return (uint32_t)kParams; }
 
 extern "C" rt_status rt_cache_init(rt_context *ctx, rt_stream stream, void *cache, const rt_cache_config *cfg) {
     if (!ctx || !cache || !cfg) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_init: null argument");
+    if (reinterpret_cast<uintptr_t>(cache) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_init: cache must be 256-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int rc = set_smem(ctx);
     if (rc) return rc;
@@ -899,6 +904,7 @@ extern "C" rt_status rt_cache_init(rt_context *ctx, rt_stream stream, void *cach
 extern "C" rt_status rt_cache_query(rt_context *ctx, rt_stream stream, const void *cache, const rt_cache_input *in,
                                     float *out, uint32_t n) {
     if (!ctx || !cache || (n && (!in || !out))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_query: null argument");
+    if (reinterpret_cast<uintptr_t>(cache) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_query: cache must be 256-byte aligned");
     if (n == 0) return RT_OK;
     int rc = set_smem(ctx);
     if (rc) return rc;
@@ -914,6 +920,7 @@ extern "C" rt_status rt_cache_query(rt_context *ctx, rt_stream stream, const voi
 extern "C" rt_status rt_cache_train(rt_context *ctx, rt_stream stream, void *cache, const rt_cache_input *in,
                                     const float *targets, uint32_t n, uint32_t batch, float *loss_out) {
     if (!ctx || !cache || (n && (!in || !targets))) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_train: null argument");
+    if (reinterpret_cast<uintptr_t>(cache) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_train: cache must be 256-byte aligned");
     if (batch == 0 || batch % 64u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_train: batch must be a positive multiple of 64");
     int rc = set_smem(ctx);
     if (rc) return rc;
@@ -933,6 +940,7 @@ extern "C" rt_status rt_cache_gradient(rt_context *ctx, rt_stream stream, void *
                                        const float *targets, uint32_t n, float *grad_out) {
     if (!ctx || !cache || !grad_out || (n && (!in || !targets)))
         return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_gradient: null argument");
+    if (reinterpret_cast<uintptr_t>(cache) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_gradient: cache must be 256-byte aligned");
     int rc = set_smem(ctx);
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -956,6 +964,7 @@ extern "C" rt_status rt_cache_get_params(rt_context *ctx, rt_stream stream, cons
 
 extern "C" rt_status rt_cache_set_params(rt_context *ctx, rt_stream stream, void *cache, const float *params) {
     if (!ctx || !cache || !params) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_set_params: null argument");
+    if (reinterpret_cast<uintptr_t>(cache) & 255u) return set_error(ctx, RT_ERR_INVALID_ARG, "rt_cache_set_params: cache must be 256-byte aligned");
     CacheState *S = static_cast<CacheState *>(cache);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     RT_CUDA_CTX(ctx, cudaMemcpyAsync(S->params, params, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));

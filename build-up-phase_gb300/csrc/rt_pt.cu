@@ -756,6 +756,8 @@ int path_trace_impl(rt_context *ctx, rt_stream stream, const rt_pt_scene *scene,
     if (cp && (!cp->cache || cp->train_paths == 0 || (cp->train_batch % 64u) != 0u))
         return set_error(ctx, RT_ERR_INVALID_ARG,
                          "rt_path_trace_cached: cache, train_paths > 0 and a train_batch multiple of 64 are required");
+    if (cp && (reinterpret_cast<uintptr_t>(cp->cache) & 255u))
+        return set_error(ctx, RT_ERR_INVALID_ARG, "rt_path_trace_cached: cache must be 256-byte aligned");
     const uint64_t npix = (uint64_t)p->width * p->height;
     if (npix == 0 || p->spp == 0) return RT_OK;
     if (npix > (1u << 30)) return set_error(ctx, RT_ERR_UNSUPPORTED, "rt_path_trace: more than 2^30 pixels");

@@ -8,7 +8,7 @@
 // Algorithm: Adinets & Merrill, "Onesweep: A Faster Least Significant Digit
 // Radix Sort for GPUs" (2022).  One histogram kernel counts the 8-bit digits
 // of every pass in a single read; each pass is then one kernel in which tiles
-// rank their keys locally (warp match_any multisplit), publish per-digit
+// rank their keys locally (warp multisplit by ballots), publish per-digit
 // counts, resolve their global offsets by decoupled look-back over earlier
 // tiles, and scatter through shared memory.  Tiles are numbered in launch
 // order by an atomic counter, so a tile only waits on tiles already owned by
@@ -32,6 +32,10 @@ constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
+// Statuses read per look-back round trip.  Tiles of one wave publish their
+// aggregates at about the same time, so a walk of one predecessor per round
+// trip crossed about half the wave serially.
+constexpr int kLookWindow = 8;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagIncl = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
@@ -94,7 +98,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
                                                             const uint32_t *__restrict__ hist,
                                                             uint32_t *__restrict__ status,
                                                             uint32_t *__restrict__ tile_counter, uint32_t *err,
-                                                            uint32_t spin_limit) {
+                                                            uint32_t spin_limit, uint32_t withhold) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(smem);
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + kSortTile);
@@ -123,27 +127,40 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
         v[j] = valid ? vin[idx] : 0u;
     }
     const uint32_t lt = (1u << lane) - 1u;
+    // Peers of each key (the valid lanes holding the same digit) from eight
+    // ballots on the digit's bits: vote instructions in registers, where
+    // match.any took about 0.5 us per round with a warp's ~30 distinct
+    // digits (7.7 of a tile's 17 us).  Eight keys per group: their peer
+    // masks first, then the leaders' shared-memory atomics back to back
+    // (applied in issue order, which keeps the ranks in input order), then
+    // the shuffles of the old counts, so no key waits on the one before it.
 #pragma unroll
-    for (int j = 0; j < kSortItems; ++j) {
-        uint32_t idx = wbase + (uint32_t)j * 32u + (uint32_t)lane;
-        bool valid = idx < n;
-        uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-        uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
-        uint32_t old = 0, below = 0;
-        int leader = lane;
-        if (valid) {
-            uint32_t peers = __match_any_sync(vmask, d);
-            leader = __ffs(peers) - 1;
-            below = __popc(peers & lt);
-            if (lane == leader) {
-                old = s_whist[w * kRadix + d];
-                s_whist[w * kRadix + d] = old + (uint32_t)__popc(peers);
+    for (int j0 = 0; j0 < kSortItems; j0 += 8) {
+        uint32_t pm[8], old[8];
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            const int j = j0 + jj;
+            const uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
+            uint32_t peers = __ballot_sync(0xffffffffu, wbase + (uint32_t)j * 32u + (uint32_t)lane < n);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t bb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+                peers &= ((d >> b) & 1u) ? bb : ~bb;
             }
+            pm[jj] = peers;
         }
-        __syncwarp();
-        old = __shfl_sync(0xffffffffu, old, leader);
-        rank[j] = old + below;
-        __syncwarp();
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            const uint32_t d = (uint32_t)(k[j0 + jj] >> shift) & dmask;
+            old[jj] = 0u;
+            if ((int)(__ffs(pm[jj]) - 1) == lane)
+                old[jj] = atomicAdd(&s_whist[w * kRadix + d], (uint32_t)__popc(pm[jj]));
+        }
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            const int leader = pm[jj] ? __ffs(pm[jj]) - 1 : lane;
+            rank[j0 + jj] = __shfl_sync(0xffffffffu, old[jj], leader) + (uint32_t)__popc(pm[jj] & lt);
+        }
     }
     __syncthreads();
 
@@ -165,14 +182,31 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
         volatile uint32_t *st = status;
         uint32_t prefix = 0;
         if (tile == 0) {
-            st[t] = kFlagIncl | total;
+            if (!withhold) st[t] = kFlagIncl | total;
         } else {
             st[(size_t)tile * kRadix + t] = kFlagAgg | total;
             __threadfence();
+            // kLookWindow predecessors per round trip, nearest first: their
+            // aggregates add up until an inclusive prefix ends the walk; a
+            // predecessor not yet published is polled alone (bounded).
             int64_t p = (int64_t)tile - 1;
-            while (p >= 0) {
-                uint32_t s;
-                uint32_t spins = 0;
+            bool done = false;
+            while (!done) {
+                uint32_t sw[kLookWindow];
+#pragma unroll
+                for (int i = 0; i < kLookWindow; ++i) sw[i] = p - i >= 0 ? st[(size_t)(p - i) * kRadix + t] : 0u;
+                int used = 0;
+#pragma unroll
+                for (int i = 0; i < kLookWindow; ++i) {
+                    if (done || used < i || (sw[i] & ~kValueMask) == 0u) continue;
+                    prefix += sw[i] & kValueMask;
+                    done = (sw[i] & ~kValueMask) == kFlagIncl;
+                    used = i + 1;
+                }
+                if (done) break;
+                p -= used;  // p >= 0: tile 0 publishes an inclusive prefix
+                if (used == kLookWindow) continue;
+                uint32_t s = 0u, spins = 0;
                 do {
                     s = st[(size_t)p * kRadix + t];
                 } while ((s & ~kValueMask) == 0u && ++spins < spin_limit);
@@ -180,9 +214,6 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
                     report_error(err, RT_ERR_TIMEOUT, 0x50000000u | (uint32_t)tile);
                     break;
                 }
-                prefix += s & kValueMask;
-                if ((s & ~kValueMask) == kFlagIncl) break;
-                --p;
             }
             st[(size_t)tile * kRadix + t] = kFlagIncl | ((prefix + total) & kValueMask);
         }
@@ -230,7 +261,8 @@ uint64_t sort_scratch_bytes(uint32_t n, int passes) {
 // keys0/vals0.  `keys_hist_done`: the caller already accumulated the digit
 // histograms into the scratch (fused with key generation).
 int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint32_t *vals0, uint64_t *keys1,
-               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err) {
+               uint32_t *vals1, uint32_t n, int key_bits, void *scratch, bool hist_done, uint32_t *err,
+               uint32_t withhold) {
     if (n == 0) return RT_OK;
     const int passes = (key_bits + 7) / 8;
     if (n > kValueMask) return RT_ERR_UNSUPPORTED;
@@ -260,7 +292,7 @@ int sort_pairs(const rt_context *ctx, cudaStream_t stream, uint64_t *keys0, uint
         uint32_t *vo = (p & 1) ? vals0 : vals1;
         k_onesweep<<<(unsigned)tiles, kSortThreads, kSortSmemBytes, stream>>>(
             ki, vi, ko, vo, n, 8 * p, digit_mask(key_bits, p), hist + p * kRadix, status + (size_t)p * tiles * kRadix, counters + p, err,
-            ctx->sort_spin_limit);
+            ctx->sort_spin_limit, withhold);
         RT_CUDA_TRY(cudaGetLastError());
     }
     if (passes & 1) {
@@ -290,6 +322,12 @@ extern "C" rt_status rt_debug_set_sort_spin_limit(rt_context *ctx, uint32_t spin
     return RT_OK;
 }
 
+extern "C" rt_status rt_debug_set_sort_withhold(rt_context *ctx, int withhold) {
+    if (!ctx) return RT_ERR_INVALID_ARG;
+    ctx->sort_withhold = withhold ? 1u : 0u;
+    return RT_OK;
+}
+
 extern "C" rt_status rt_sort_pairs(rt_context *ctx, rt_stream stream, uint64_t *keys, uint32_t *vals, uint32_t n,
                                    uint32_t key_bits, void *scratch, uint64_t scratch_bytes) {
     if (!ctx || (n && (!keys || !vals || !scratch)) || key_bits == 0 || key_bits > 64)
@@ -303,7 +341,7 @@ extern "C" rt_status rt_sort_pairs(rt_context *ctx, rt_stream stream, uint64_t *
     uint32_t *v1 = reinterpret_cast<uint32_t *>(s + (size_t)n * 8u);
     void *sort_s = s + rtc::align_up((uint64_t)n * 12u, 256);
     int st = rtc::sort_pairs(ctx, static_cast<cudaStream_t>(stream), keys, vals, k1, v1, n, (int)key_bits, sort_s, false,
-                             ctx->d_err);
+                             ctx->d_err, ctx->sort_withhold);
     if (st) return rtc::set_error(ctx, st, "rt_sort_pairs: launch failed");
     return RT_OK;
 }

@@ -210,6 +210,7 @@ PROTOTYPES = {
     "rt_sort_pairs": (_i32, [_vp, _vp, _vp, _vp, _u32, _u32, _vp, _u64]),
     "rt_debug_blas_scratch_layout": (_i32, [_u32, _u32, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
     "rt_debug_set_sort_spin_limit": (_i32, [_vp, _u32]),
+    "rt_debug_set_sort_withhold": (_i32, [_vp, _i32]),
     "rt_debug_host_in_place": (_i32, [_vp, _vp, _u64, C.POINTER(_i32)]),
     "rt_debug_read_sweep": (_i32, [_vp, _vp, _vp, _u64, _u32]),
     "rt_debug_pt_cache_layout": (_i32, [C.POINTER(PtParams), C.POINTER(PtCacheParams), _u32,
@@ -559,6 +560,10 @@ class Context:
     def set_sort_spin_limit(self, spins: int) -> None:
         """rt_debug_set_sort_spin_limit (0 restores the default)."""
         self.check(self.lib.rt_debug_set_sort_spin_limit(self.h, spins), "rt_debug_set_sort_spin_limit")
+
+    def set_sort_withhold(self, withhold: bool) -> None:
+        """rt_debug_set_sort_withhold: the first tile of each pass publishes no status."""
+        self.check(self.lib.rt_debug_set_sort_withhold(self.h, 1 if withhold else 0), "rt_debug_set_sort_withhold")
 
     @staticmethod
     def pt_cache_layout(params: PtParams, cp: PtCacheParams, n_lights: int) -> PtCacheLayout:

@@ -41,6 +41,14 @@ rt_status rt_debug_blas_scratch_layout(uint32_t n_tris, uint32_t flags, uint64_t
  * path; a small limit makes the sort's output wrong. */
 rt_status rt_debug_set_sort_spin_limit(rt_context *ctx, uint32_t spins);
 
+/* When `withhold` is nonzero, the first tile of every onesweep pass of this
+ * context's rt_sort_pairs calls (not its builds) publishes no status, so the tile after it waits on a
+ * status that nothing sets until its poll limit runs out (RT_ERR_TIMEOUT):
+ * a bounded wait made to expire on purpose, with every write still inside
+ * the output.  0 restores normal sorts.  For tests of the timeout path; the
+ * sort's output is wrong while it is set. */
+rt_status rt_debug_set_sort_withhold(rt_context *ctx, int withhold);
+
 /* Bandwidth probe: reads the device buffer [buf, buf + bytes) `passes` times
  * with 16-byte loads cached in L2 only; the caller times it (CUDA events on
  * `stream`).  A buffer well below the L2 size (129 MB on a GB300) measures L2

@@ -227,3 +227,30 @@ def test_checkpoint_restores_training_state(ctx, cache, tmp_path):
             ctx.cache_load(other, p2)
         assert e.value.code == rtcore.RT_ERR_INVALID_ARG
     assert host(other).tobytes() == before.tobytes()
+
+
+def test_misaligned_cache_is_rejected(ctx, cache):
+    """A cache buffer that is not 256-byte aligned is refused on the host with
+    RT_ERR_INVALID_ARG by every entry point that launches a kernel on it;
+    nothing is launched and the aligned cache is untouched."""
+    import rtcore
+    import torch
+    p0 = get_params(ctx, cache)
+    x = random_inputs(64, 8)
+    t = smooth_target(x)
+    off = torch.zeros(ctx.cache_bytes() + 256, dtype=torch.uint8, device="cuda")[16:]
+    out = torch.empty(64 * 16, dtype=torch.uint8, device="cuda")
+    g = torch.empty(rtcore.load().rt_cache_param_count() * 4, dtype=torch.uint8, device="cuda")
+    calls = [
+        lambda: ctx.cache_init(off, rtcore.cache_config(seed=7)),
+        lambda: ctx.cache_query(off, dev(x), out, 64),
+        lambda: ctx.cache_train(off, dev(x), dev(t), 64, 64),
+        lambda: ctx.cache_gradient(off, dev(x), dev(t), 64, g),
+        lambda: ctx.cache_set_params(off, dev(p0)),
+    ]
+    for call in calls:
+        with pytest.raises(rtcore.RtError) as e:
+            call()
+        assert e.value.code == rtcore.RT_ERR_INVALID_ARG
+    ctx.sync()
+    assert get_params(ctx, cache).tobytes() == p0.tobytes()

@@ -1,8 +1,9 @@
 """Failure paths of the CUDA path that need no GPU fault: a bounded
-device-side wait made to run out (the onesweep look-back of the sort), and
-the host-memory ray API refusing in-place access to a host range with an
-unmapped gap.  Nothing here faults, traps or hangs a GPU: the timeout comes
-from the library's own poll limit, and the gap is only inspected on the host."""
+device-side wait made to run out (the onesweep look-back of the sort, on a
+status that nothing sets), and the host-memory ray API refusing in-place
+access to a host range with an unmapped gap.  Nothing here faults, traps or
+hangs a GPU: the timeout comes from the library's own poll limit, and the gap
+is only inspected on the host."""
 from __future__ import annotations
 
 import ctypes as C
@@ -15,13 +16,14 @@ pytestmark = pytest.mark.gpu
 
 
 def test_sort_lookback_timeout_is_reported(ctx):
-    """With the look-back limited to one poll, tiles that find a predecessor
-    not yet published give up: rt_sync reports RT_ERR_TIMEOUT, the kernels
-    return (no write leaves the output) and the context stays usable -- the
-    next sort at the default limit is correct."""
+    """The first tile of each pass withholds its status (a flag that nothing
+    sets), so the look-back of the tile after it polls until its limit runs
+    out: rt_sync reports RT_ERR_TIMEOUT, every kernel returns (no write
+    leaves the output) and the context stays usable -- the next sort with
+    normal settings is correct."""
     import torch
     import rtcore
-    n = 1 << 21
+    n = 1 << 20
     rng = np.random.default_rng(11)
     keys = rng.integers(0, 2**63, n, dtype=np.uint64)
     vals = np.arange(n, dtype=np.uint32)
@@ -32,9 +34,10 @@ def test_sort_lookback_timeout_is_reported(ctx):
     dk = torch.from_numpy(keys.view(np.int64)).cuda()
     dv = torch.from_numpy(vals.view(np.int32)).cuda()
     codes = []
-    ctx.set_sort_spin_limit(1)
+    ctx.set_sort_spin_limit(1 << 12)
+    ctx.set_sort_withhold(True)
     try:
-        for _ in range(4):
+        for _ in range(2):
             k, v = dk.clone(), dv.clone()
             ctx.sort_pairs(k, v, n, 64, scratch, nb)
             try:
@@ -43,10 +46,10 @@ def test_sort_lookback_timeout_is_reported(ctx):
             except rtcore.RtError as e:
                 codes.append(e.code)
     finally:
+        ctx.set_sort_withhold(False)
         ctx.set_sort_spin_limit(0)
-    print(f"statuses with a one-poll look-back: {codes}")
-    assert set(codes) <= {0, rtcore.RT_ERR_TIMEOUT}, codes
-    assert rtcore.RT_ERR_TIMEOUT in codes, "no look-back ran out with a limit of one poll"
+    print(f"statuses with the first tile's status withheld: {codes}")
+    assert codes == [rtcore.RT_ERR_TIMEOUT] * 2, codes
     k, v = dk.clone(), dv.clone()
     ctx.sort_pairs(k, v, n, 64, scratch, nb)
     ctx.sync()
@@ -54,6 +57,7 @@ def test_sort_lookback_timeout_is_reported(ctx):
     assert np.array_equal(k.cpu().numpy().view(np.uint64), keys[order])
     assert np.array_equal(v.cpu().numpy().view(np.uint32), vals[order])
     assert rtcore.load().rt_debug_set_sort_spin_limit(None, 1) == rtcore.RT_ERR_INVALID_ARG
+    assert rtcore.load().rt_debug_set_sort_withhold(None, 1) == rtcore.RT_ERR_INVALID_ARG
 
 
 def test_host_range_with_unmapped_gap_is_staged(ctx):
