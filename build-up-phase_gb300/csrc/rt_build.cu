@@ -461,8 +461,7 @@ __device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p) {
 // One thread per leaf climbs towards the root; the second thread to arrive
 // at a node computes it.  The climbing thread keeps its own subtree's box and
 // cost in registers and loads only the sibling's; the node's children and
-// parent (read-only here) are loaded before the arrival so their latency
-// overlaps the atomic.
+// parent (read-only here) come from the previous level's loads.
 __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.n) return;
@@ -473,6 +472,15 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
     Box mb = lb;
     float mcost = RT_SAH_PRIM;
     uint32_t p = __ldg(a.parent + a.n - 1 + j);
+    // p's children and parent, loaded one level ahead: each level costs the
+    // arrival and one round of loads (the sibling's box and cost with the
+    // next level's node), not a third round trip for the node itself
+    uint4 nd = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t pp = kNone;
+    if (p < a.n - 1) {
+        nd = __ldg(a.bin + p);
+        pp = __ldg(a.parent + p);
+    }
     // A radix tree over 2^30 keys is at most 96 levels deep (63 key bits +
     // 32 index bits); the cap only guards against a corrupt parent chain.
     for (int climb = 0; p != kNone; ++climb) {
@@ -480,9 +488,13 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
             report_error(a.err, RT_ERR_BOUNDS, 0x61000000u | j);
             return;
         }
-        const uint4 nd = __ldg(a.bin + p);
-        const uint32_t pp = __ldg(a.parent + p);
         if (arrive_acq_rel(a.visit + p) == 0u) return;
+        uint4 nd_next = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t pp_next = kNone;
+        if (pp < a.n - 1) {
+            nd_next = __ldg(a.bin + pp);
+            pp_next = __ldg(a.parent + pp);
+        }
         const bool left = nd.x == me;
         const uint32_t sib = left ? nd.y : nd.x;
         const bool sl = (sib & kLeafBit) != 0u;
@@ -509,6 +521,8 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
         mb = b;
         me = p;
         p = pp;
+        nd = nd_next;
+        pp = pp_next;
     }
 }
 
