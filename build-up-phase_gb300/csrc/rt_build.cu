@@ -600,6 +600,17 @@ __device__ __forceinline__ RefInfo fetch_ref(const CollapseArgs &a, uint32_t r) 
 }
 __device__ __forceinline__ bool info_open(const RefInfo &x) { return (x.cnt & kOpenBit) != 0u; }
 
+// RefInfo of lane `src` (every lane of the warp takes part).
+__device__ __forceinline__ RefInfo shfl_info(const RefInfo &x, int src) {
+    RefInfo y;
+    y.ref = __shfl_sync(0xffffffffu, x.ref, src);
+    y.kid0 = __shfl_sync(0xffffffffu, x.kid0, src);
+    y.kid1 = __shfl_sync(0xffffffffu, x.kid1, src);
+    y.cnt = __shfl_sync(0xffffffffu, x.cnt, src);
+    y.area = __shfl_sync(0xffffffffu, x.area, src);
+    return y;
+}
+
 // Quantisation frame of a wide node: the origin (lower corner) and per-axis
 // power-of-two scales of its 8-bit child boxes.
 struct QFrame {
@@ -676,8 +687,9 @@ __device__ void encode_node(const Box &node, const Box sbox[8], const bool used[
 // Phase A, eight lanes per wide node.  Lane j of an aligned group of eight
 // holds child j during the widening and the slot assignment, and the group's
 // choices are made with shuffles (every lane reaches the same result), so a
-// node costs one round trip per widening step and a few hundred instructions
-// per lane.  Every loop that shuffles is warp-uniform: all 32 lanes run each
+// node costs a round trip per level of its treelet's top three binary levels
+// (fetched before the widening), one per node opened below them, and a few
+// hundred instructions per lane.  Every loop that shuffles is warp-uniform: all 32 lanes run each
 // shuffle, groups that are done (or hold no node) take part with `act` off.
 // ---------------------------------------------------------------------------
 
@@ -729,7 +741,7 @@ __device__ __forceinline__ int group_argmin(float key, bool ok) {
 // (bits 0-7) and each leaf slot's primitive count minus one (two bits per
 // slot from bit 8).  Returns the node's internal children and primitives
 // (every lane of the group).
-__device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, uint32_t &n_int, uint32_t &n_prim) {
+__device__ __forceinline__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, uint32_t &n_int, uint32_t &n_prim) {
     const int j = (int)(threadIdx.x & 7u);
     const int gb = (int)(threadIdx.x & 24u);
     // wq and the hand-off arrays are written by other blocks of this launch
@@ -740,46 +752,72 @@ __device__ void collapse_phase_a(const CollapseArgs &a, uint32_t k, bool valid, 
         sref = __ldcg(a.wq + k);
         src = fetch_ref(a, sref);
     }
-    // mine: this lane's child; pre0/pre1: its binary children, fetched as
-    // soon as the child is known to be openable, so that opening it later
-    // (usually a step or more afterwards) finds them already loaded.
-    RefInfo mine = {0u, 0u, 0u, 0u, 0.0f}, pre0 = mine, pre1 = mine;
+    // The treelet's top three binary levels are fetched up front, one round
+    // trip per level for the whole group: t1 (lanes 0-1), t2 (lanes 0-3) and
+    // t3 (lanes 0-7) hold the nodes at depth 1, 2 and 3 below the wide
+    // node's root, node i's children at 2i and 2i + 1 of the next depth
+    // (empty where the parent is not opened).  The widening then finds the
+    // children of an opened node in these tables by shuffles; only a node
+    // opened below depth 3 has its children fetched when it is opened.
+    const bool src_open = valid && info_open(src);
+    RefInfo t1 = {0u, 0u, 0u, 0u, 0.0f}, t2 = t1, t3 = t1;
+    if (src_open && j < 2) t1 = fetch_ref(a, j == 0 ? src.kid0 : src.kid1);
+    {
+        const RefInfo par = shfl_info(t1, gb | ((j >> 1) & 1));
+        if (src_open && j < 4 && info_open(par)) t2 = fetch_ref(a, (j & 1) ? par.kid1 : par.kid0);
+    }
+    {
+        const RefInfo par = shfl_info(t2, gb | ((j >> 1) & 3));
+        if (src_open && info_open(par)) t3 = fetch_ref(a, (j & 1) ? par.kid1 : par.kid0);
+    }
+    // mine: this lane's child, at depth mdepth (4: below the tables) and
+    // index midx of its depth
+    RefInfo mine = {0u, 0u, 0u, 0u, 0.0f};
+    uint32_t mdepth = 0u, midx = 0u;
     int n = 0;
     if (valid) {
-        if (!info_open(src)) {
+        if (!src_open) {
             n = 1;
             if (j == 0) mine = src;
         } else {
             n = 2;
-            if (j < 2) mine = fetch_ref(a, j == 0 ? src.kid0 : src.kid1);
+            if (j < 2) {
+                mine = t1;
+                mdepth = 1u;
+                midx = (uint32_t)j;
+            }
         }
     }
-    if (valid && j < n && n < (int)a.width && info_open(mine)) {
-        pre0 = fetch_ref(a, mine.kid0);
-        pre1 = fetch_ref(a, mine.kid1);
-    }
-    bool act = valid && info_open(src);
+    bool act = src_open;
     for (;;) {
         act = act && n < (int)a.width;
         if (!__any_sync(kFullMask, act)) break;
         const int best = group_argmax(mine.area, act && j < n && info_open(mine) && mine.area > -1.0f);
         const int from = gb | (best < 0 ? 0 : best);
-        RefInfo moved;
-        moved.ref = __shfl_sync(kFullMask, pre1.ref, from);
-        moved.kid0 = __shfl_sync(kFullMask, pre1.kid0, from);
-        moved.kid1 = __shfl_sync(kFullMask, pre1.kid1, from);
-        moved.cnt = __shfl_sync(kFullMask, pre1.cnt, from);
-        moved.area = __shfl_sync(kFullMask, pre1.area, from);
         if (best < 0) act = false;
+        // the opened child's depth and index (the same on every lane of the group)
+        const uint32_t bd = __shfl_sync(kFullMask, mdepth, from);
+        const uint32_t bi = __shfl_sync(kFullMask, midx, from);
+        const bool deep = bd >= 3u;
+        RefInfo f0 = {0u, 0u, 0u, 0u, 0.0f}, f1 = f0;
+        if (act && deep && j == best) {
+            f0 = fetch_ref(a, mine.kid0);
+            f1 = fetch_ref(a, mine.kid1);
+        }
+        const RefInfo tab = bd == 1u ? t2 : t3;
+        const RefInfo k0 = shfl_info(deep ? f0 : tab, deep ? from : (gb | (int)((2u * bi) & 7u)));
+        const RefInfo k1 = shfl_info(deep ? f1 : tab, deep ? from : (gb | (int)((2u * bi + 1u) & 7u)));
         if (act) {
-            const bool fresh = j == best || j == n;
-            if (j == best) mine = pre0;
-            else if (j == n) mine = moved;
-            ++n;
-            if (fresh && n < (int)a.width && info_open(mine)) {
-                pre0 = fetch_ref(a, mine.kid0);
-                pre1 = fetch_ref(a, mine.kid1);
+            if (j == best) {
+                mine = k0;
+                mdepth = deep ? 4u : bd + 1u;
+                midx = 2u * bi;
+            } else if (j == n) {
+                mine = k1;
+                mdepth = deep ? 4u : bd + 1u;
+                midx = 2u * bi + 1u;
             }
+            ++n;
         }
     }
 
@@ -929,6 +967,28 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *s_red) {
     return s;
 }
 
+// Block-wide sums of four values at once (one shared-memory round instead
+// of four).
+template <int N>
+__device__ __forceinline__ uint4 block_sum4(uint4 v, uint4 *s_red4) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+        v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
+    }
+    if ((threadIdx.x & 31) == 0) s_red4[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint4 s = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = 0; i < N / 32; ++i) {
+        const uint4 c = s_red4[i];
+        s.x += c.x; s.y += c.y; s.z += c.z; s.w += c.w;
+    }
+    __syncthreads();
+    return s;
+}
+
 template <int N>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_red, uint32_t &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -988,8 +1048,9 @@ __device__ bool coop_sync(uint32_t *bar, uint32_t nblocks, uint32_t *err, uint32
     return s_ok != 0;
 }
 
-__global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
+__global__ void __launch_bounds__(kCollapseThreads, 4) k_collapse(CollapseArgs a) {
     __shared__ uint32_t s_red[kCollapseThreads / 32];
+    __shared__ uint4 s_red4[kCollapseThreads / 32];
     const uint32_t G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
     if (b == 0 && t == 0) a.wq[0] = a.root_ref;
     if (!coop_sync(a.bar, G, a.err, 0x64000000u)) return;
@@ -1018,8 +1079,11 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
                 my_prim += np;
             }
         }
-        my_int = block_sum<kCollapseThreads>(my_int, s_red);
-        my_prim = block_sum<kCollapseThreads>(my_prim, s_red);
+        {
+            const uint4 bs = block_sum4<kCollapseThreads>(make_uint4(my_int, my_prim, 0u, 0u), s_red4);
+            my_int = bs.x;
+            my_prim = bs.y;
+        }
         if (t == 0) { a.blk[2 * b] = my_int; a.blk[2 * b + 1] = my_prim; }
         if (!coop_sync(a.bar, G, a.err, 0x64000000u | depth)) return;
         uint32_t pre_i = 0, pre_p = 0, tot_i = 0, tot_p = 0;
@@ -1029,10 +1093,13 @@ __global__ void __launch_bounds__(kCollapseThreads) k_collapse(CollapseArgs a) {
             tot_p += vp;
             if (q < b) { pre_i += vi; pre_p += vp; }
         }
-        pre_i = block_sum<kCollapseThreads>(pre_i, s_red);
-        pre_p = block_sum<kCollapseThreads>(pre_p, s_red);
-        tot_i = block_sum<kCollapseThreads>(tot_i, s_red);
-        tot_p = block_sum<kCollapseThreads>(tot_p, s_red);
+        {
+            const uint4 bs = block_sum4<kCollapseThreads>(make_uint4(pre_i, pre_p, tot_i, tot_p), s_red4);
+            pre_i = bs.x;
+            pre_p = bs.y;
+            tot_i = bs.z;
+            tot_p = bs.w;
+        }
         const uint32_t next_start = level_start + level_count;
         uint32_t run_i = pre_i, run_p = pre_p;
         for (uint32_t kb = c0; kb < c1; kb += kCollapseThreads) {
