@@ -10,9 +10,10 @@
 //   morton    30- or 63-bit Morton code of each box centre, fused with the
 //             digit histograms of the radix sort
 //   sort      onesweep LSD radix sort (rt_sort.cu), stable
-//   karras    binary radix tree over the sorted keys (Karras, HPG 2012),
-//             index-augmented keys for duplicates
-//   refit     bottom-up boxes + SAH leaf decisions (one atomic per node)
+//   tree      binary radix tree over the sorted keys (Karras, HPG 2012;
+//             index-augmented keys for duplicates), built bottom-up as in
+//             Apetrei (2014) together with the boxes and SAH leaf decisions
+//             (one exchange per node)
 //   collapse  one cooperative kernel, breadth-first level by level, eight
 //             lanes per wide node: greedy widening to 8 children, octant slot
 //             assignment, 8-bit child-box quantisation (Ylitie, Karras,
@@ -43,7 +44,7 @@ struct GeomParams {
 };
 
 struct BuildLayout {
-    uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, parent, node_box, node_cost, leafable, visit, leaf_box,
+    uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, node_box, node_cost, leafable, visit, leaf_box,
         wq, slots, desc, counts, blk, misc, sort, total;
 };
 
@@ -73,11 +74,10 @@ BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
     L.ids0 = take((uint64_t)n * 4u);
     L.ids1 = take((uint64_t)n * 4u);
     L.bin = take(ni * 16u);
-    L.parent = take((ni + n) * 4u);
     L.node_box = take(ni * 32u);
     L.node_cost = take(ni * 4u);
     L.leafable = take(ni);
-    L.visit = take(ni * 4u);
+    L.visit = take(ni * 8u);
     L.leaf_box = take((uint64_t)n * 32u);
     L.wq = take(cap * 4u);
     L.slots = take(cap * 32u);
@@ -390,113 +390,91 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ boxes,
 }
 
 // ---------------------------------------------------------------------------
-// karras
+// Radix tree + refit + SAH leaf decisions in one pass
 // ---------------------------------------------------------------------------
+//
+// The binary radix tree over the sorted keys (Karras 2012: every internal
+// node splits its key range where the keys' common prefix ends, equal keys
+// ordered by index) built bottom-up as in Apetrei 2014 ("Fast and Simple
+// Agglomerative LBVH Construction"): one thread per leaf climbs; a node
+// covering keys [l, r] is the left child of the node split between keys r
+// and r + 1, or the right child of the node split between l - 1 and l --
+// whichever boundary's keys share the longer prefix (never equal: the keys
+// are unique with their indices).  Internal node i is the one split between
+// keys i and i + 1.  The first child to reach a node exchanges its reference
+// and the far end of its range into the node's 64-bit word; the second child
+// gets them back, so it knows its sibling and the node's range, and
+// computes the node: box, SAH cost and the leaf decision (the refit), then
+// climbs on.  Same tree as a top-down Karras construction, in one launch and
+// without its per-node searches.
 
-__device__ __forceinline__ int kdelta(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
-    if (j < 0 || j >= n) return -1;
-    uint64_t a = k[i], b = k[j];
-    if (a == b) return 64 + __clz((int)((uint32_t)i ^ (uint32_t)j));
-    return __clzll((long long)(a ^ b));
+// Common-prefix length of the keys on either side of boundary b | b + 1, the
+// index breaking ties between equal keys.
+__device__ __forceinline__ int boundary_delta(uint64_t ka, uint64_t kb, uint32_t b) {
+    if (ka == kb) return 64 + __clz((int)(b ^ (b + 1u)));
+    return __clzll((long long)(ka ^ kb));
 }
 
-__global__ void __launch_bounds__(256) k_karras(const uint64_t *__restrict__ k, uint32_t n, uint4 *__restrict__ bin,
-                                                 uint32_t *__restrict__ parent) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t N = n;
-    if (i >= N - 1) return;
-    if (i == 0) parent[0] = kNone;
-    int d = (kdelta(k, N, i, i + 1) - kdelta(k, N, i, i - 1)) > 0 ? 1 : -1;
-    int dmin = kdelta(k, N, i, i - d);
-    int64_t lmax = 2;
-    while (kdelta(k, N, i, i + lmax * d) > dmin) lmax <<= 1;
-    int64_t l = 0;
-    for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
-        if (kdelta(k, N, i, i + (l + t) * d) > dmin) l += t;
-    int64_t j = i + l * d;
-    int dnode = kdelta(k, N, i, j);
-    int64_t s = 0, t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (kdelta(k, N, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    int64_t gamma = i + s * d + min(d, 0);
-    int64_t lo = min(i, j), hi = max(i, j);
-    uint32_t left = (lo == gamma) ? (kLeafBit | (uint32_t)gamma) : (uint32_t)gamma;
-    uint32_t right = (hi == gamma + 1) ? (kLeafBit | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
-    bin[i] = make_uint4(left, right, (uint32_t)lo, (uint32_t)hi);
-    // parents: internal x at parent[x], leaf y at parent[n - 1 + y]
-    parent[(left & kLeafBit) ? (N - 1 + (left & ~kLeafBit)) : left] = (uint32_t)i;
-    parent[(right & kLeafBit) ? (N - 1 + (right & ~kLeafBit)) : right] = (uint32_t)i;
-}
-
-// ---------------------------------------------------------------------------
-// refit + SAH
-// ---------------------------------------------------------------------------
-
-struct RefitArgs {
+struct TreeArgs {
     uint32_t n;
-    const uint32_t *ids;
+    const uint64_t *keys;  // sorted
+    const uint32_t *ids;   // build-input primitive of each sorted key
     const float *boxes;
-    const uint32_t *parent;
-    const uint4 *bin;
+    uint4 *bin;            // internal node i: left, right, first, last
     float *node_box;
     float *node_cost;
     uint8_t *leafable;
-    uint32_t *visit;
+    uint64_t *other;       // per internal node: all ones, then the first child's reference and far end
     float *leaf_box;
+    uint32_t *root;        // the root's reference
     uint32_t *err;
 };
 
-// Arrival at a binary node: increments its counter with release (this
-// thread's earlier stores -- its subtree's box and cost -- are visible to the
-// thread that reads the new value) and acquire (the first arrival's stores
-// are visible to this thread's later loads) at device scope.
-__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p) {
-    uint32_t old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+// Exchange with release (this thread's box and cost stores are visible to
+// the thread that reads the value) and acquire (the first child's stores are
+// visible to this thread's later loads) at device scope.
+__device__ __forceinline__ uint64_t exch_acq_rel(uint64_t *p, uint64_t v) {
+    uint64_t old;
+    asm volatile("atom.acq_rel.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     return old;
 }
 
-// One thread per leaf climbs towards the root; the second thread to arrive
-// at a node computes it.  The climbing thread keeps its own subtree's box and
-// cost in registers and loads only the sibling's; the node's children and
-// parent (read-only here) come from the previous level's loads.
-__global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
-    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.n) return;
-    const Box lb = load_box(a.boxes, a.ids[j]);
+__global__ void __launch_bounds__(256) k_tree(TreeArgs a) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = a.n;
+    if (j >= n) return;
+    // the leaf's box and the keys around its range, in one round of loads
+    const uint32_t id = __ldg(a.ids + j);
+    uint64_t kl = __ldg(a.keys + j), kr = kl;
+    uint64_t klm = j > 0 ? __ldg(a.keys + j - 1) : 0ull, krp = j + 1 < n ? __ldg(a.keys + j + 1) : 0ull;
+    const Box lb = load_box(a.boxes, id);
     store_box(a.leaf_box, j, lb);
-    if (a.n < 2) return;
-    uint32_t me = kLeafBit | j;
+    if (n < 2) return;
+    uint32_t me = kLeafBit | j, l = j, r = j;
     Box mb = lb;
     float mcost = RT_SAH_PRIM;
-    uint32_t p = __ldg(a.parent + a.n - 1 + j);
-    // p's children and parent, loaded one level ahead: each level costs the
-    // arrival and one round of loads (the sibling's box and cost with the
-    // next level's node), not a third round trip for the node itself
-    uint4 nd = make_uint4(0u, 0u, 0u, 0u);
-    uint32_t pp = kNone;
-    if (p < a.n - 1) {
-        nd = __ldg(a.bin + p);
-        pp = __ldg(a.parent + p);
-    }
     // A radix tree over 2^30 keys is at most 96 levels deep (63 key bits +
-    // 32 index bits); the cap only guards against a corrupt parent chain.
-    for (int climb = 0; p != kNone; ++climb) {
-        if (climb >= 256 || p >= a.n - 1) {
+    // 32 index bits); the cap only guards against inconsistent keys.
+    for (int climb = 0;; ++climb) {
+        if (climb >= 256) {
             report_error(a.err, RT_ERR_BOUNDS, 0x61000000u | j);
             return;
         }
-        if (arrive_acq_rel(a.visit + p) == 0u) return;
-        uint4 nd_next = make_uint4(0u, 0u, 0u, 0u);
-        uint32_t pp_next = kNone;
-        if (pp < a.n - 1) {
-            nd_next = __ldg(a.bin + pp);
-            pp_next = __ldg(a.parent + pp);
+        const bool left = l == 0u ? true : (r == n - 1u ? false : boundary_delta(kr, krp, r) > boundary_delta(klm, kl, l - 1u));
+        const uint32_t p = left ? r : l - 1u;
+        const uint64_t got = exch_acq_rel(a.other + p, ((uint64_t)me << 32) | (left ? l : r));
+        if (got == ~0ull) return;  // first child here: the sibling computes the node
+        const uint32_t sib = (uint32_t)(got >> 32), far = (uint32_t)got;
+        const uint32_t nl = left ? l : far, nr = left ? far : r;
+        if (nl > nr || nr >= n) {
+            report_error(a.err, RT_ERR_BOUNDS, 0x61000000u | j);
+            return;
         }
-        const bool left = nd.x == me;
-        const uint32_t sib = left ? nd.y : nd.x;
+        // the sibling's box and cost and the keys around the node's range,
+        // in one round of loads
+        const uint64_t k_nl = left ? kl : __ldg(a.keys + nl), k_nr = left ? __ldg(a.keys + nr) : kr;
+        const uint64_t k_nlm = nl > 0u ? __ldg(a.keys + nl - 1u) : 0ull;
+        const uint64_t k_nrp = nr + 1u < n ? __ldg(a.keys + nr + 1u) : 0ull;
         const bool sl = (sib & kLeafBit) != 0u;
         const Box sb = sl ? load_box(a.leaf_box, sib & ~kLeafBit) : load_box(a.node_box, sib);
         const float scost = sl ? RT_SAH_PRIM : __ldcg(a.node_cost + sib);
@@ -511,18 +489,26 @@ __global__ void __launch_bounds__(256) k_refit(RefitArgs a) {
         } else {
             split = RT_SAH_NODE + (cl + cr);
         }
-        const uint32_t count = nd.w - nd.z + 1u;
+        const uint32_t count = nr - nl + 1u;
         const float leaf = (float)count * RT_SAH_PRIM;
         const bool lf = count <= (uint32_t)RT_MAX_LEAF_PRIMS && leaf <= split;
         mcost = lf ? leaf : split;
         store_box(a.node_box, p, b);
         a.node_cost[p] = mcost;
         a.leafable[p] = lf ? 1 : 0;
+        a.bin[p] = make_uint4(left ? me : sib, left ? sib : me, nl, nr);
         mb = b;
         me = p;
-        p = pp;
-        nd = nd_next;
-        pp = pp_next;
+        l = nl;
+        r = nr;
+        kl = k_nl;
+        kr = k_nr;
+        klm = k_nlm;
+        krp = k_nrp;
+        if (l == 0u && r == n - 1u) {
+            *a.root = p;
+            return;
+        }
     }
 }
 
@@ -535,6 +521,7 @@ struct CollapseArgs {
     uint32_t width;      // children per wide node, 4..8
     uint32_t capacity;
     uint32_t root_ref;
+    const uint32_t *root_dev;  // when set: the root's reference, read on the device
     uint32_t *gather;  // per leaf record in node order: its sorted primitive
     const uint4 *bin;
     const float *node_box;
@@ -1052,7 +1039,8 @@ __global__ void __launch_bounds__(kCollapseThreads, 4) k_collapse(CollapseArgs a
     __shared__ uint32_t s_red[kCollapseThreads / 32];
     __shared__ uint4 s_red4[kCollapseThreads / 32];
     const uint32_t G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
-    if (b == 0 && t == 0) a.wq[0] = a.root_ref;
+    const uint32_t root_ref = a.root_dev ? __ldcg(a.root_dev) : a.root_ref;
+    if (b == 0 && t == 0) a.wq[0] = root_ref;
     if (!coop_sync(a.bar, G, a.err, 0x64000000u)) return;
     uint32_t level_start = 0, level_count = 1, prim_next = 0, depth = 0;
     // Every block evaluates the same level sizes, so all leave together; the
@@ -1120,7 +1108,7 @@ __global__ void __launch_bounds__(kCollapseThreads, 4) k_collapse(CollapseArgs a
         if (!coop_sync(a.bar, G, a.err, 0x65000000u | depth)) return;
     }
     if (b == 0 && t == 0) {
-        Box rb = ref_box(a, a.root_ref);
+        Box rb = ref_box(a, root_ref);
         a.hdr->node_count = level_start;
         a.hdr->depth = depth;
         for (int q = 0; q < 3; ++q) { a.hdr->bounds_lo[q] = rb.lo[q]; a.hdr->bounds_hi[q] = rb.hi[q]; }
@@ -1246,37 +1234,35 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     if (sst) return set_error(ctx, sst, "radix sort launch failed");
 
     uint4 *bin = reinterpret_cast<uint4 *>(S + L.bin);
-    uint32_t *parent = reinterpret_cast<uint32_t *>(S + L.parent);
-    if (n >= 2) {
-        k_karras<<<(n - 1 + 255u) / 256u, 256, 0, st>>>(keys0, n, bin, parent);
-        RT_CUDA_CTX(ctx, cudaGetLastError());
-        RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.visit, 0, (size_t)(n - 1) * 4u, st));
-    }
-    RefitArgs ra;
-    ra.n = n;
-    ra.ids = ids0;
-    ra.boxes = boxes;
-    ra.parent = parent;
-    ra.bin = bin;
-    ra.node_box = reinterpret_cast<float *>(S + L.node_box);
-    ra.node_cost = reinterpret_cast<float *>(S + L.node_cost);
-    ra.leafable = reinterpret_cast<uint8_t *>(S + L.leafable);
-    ra.visit = reinterpret_cast<uint32_t *>(S + L.visit);
-    ra.leaf_box = reinterpret_cast<float *>(S + L.leaf_box);
-    ra.err = ctx->d_err;
-    k_refit<<<nb, 256, 0, st>>>(ra);
+    uint32_t *root_word = reinterpret_cast<uint32_t *>(S + L.misc + 64u);
+    if (n >= 2) RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.visit, 0xff, (size_t)(n - 1) * 8u, st));
+    TreeArgs ta;
+    ta.n = n;
+    ta.keys = keys0;
+    ta.ids = ids0;
+    ta.boxes = boxes;
+    ta.bin = bin;
+    ta.node_box = reinterpret_cast<float *>(S + L.node_box);
+    ta.node_cost = reinterpret_cast<float *>(S + L.node_cost);
+    ta.leafable = reinterpret_cast<uint8_t *>(S + L.leafable);
+    ta.other = reinterpret_cast<uint64_t *>(S + L.visit);
+    ta.leaf_box = reinterpret_cast<float *>(S + L.leaf_box);
+    ta.root = root_word;
+    ta.err = ctx->d_err;
+    k_tree<<<nb, 256, 0, st>>>(ta);
     RT_CUDA_CTX(ctx, cudaGetLastError());
 
     CollapseArgs ca;
     ca.n = n;
     ca.width = build_width(bc.flags);
     ca.capacity = cap;
-    ca.root_ref = n >= 2 ? 0u : (kLeafBit | 0u);
+    ca.root_ref = kLeafBit | 0u;                    // one primitive: the root is leaf 0
+    ca.root_dev = n >= 2 ? root_word : nullptr;   // otherwise the node k_tree found
     ca.gather = ids1;  // free once the sort has left its result in keys0/ids0
     ca.bin = bin;
-    ca.node_box = ra.node_box;
-    ca.leafable = ra.leafable;
-    ca.leaf_box = ra.leaf_box;
+    ca.node_box = ta.node_box;
+    ca.leafable = ta.leafable;
+    ca.leaf_box = ta.leaf_box;
     ca.wq = reinterpret_cast<uint32_t *>(S + L.wq);
     ca.slots = reinterpret_cast<uint32_t *>(S + L.slots);
     ca.desc = reinterpret_cast<uint32_t *>(S + L.desc);

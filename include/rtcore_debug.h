@@ -29,7 +29,8 @@ rt_status rt_sort_pairs(rt_context *ctx, rt_stream stream, uint64_t *keys, uint3
 /* Byte offsets, within the scratch buffer of a finished BLAS build of n_tris
  * triangles, of the sorted Morton keys (uint64), the sorted build-input
  * triangle ids (uint32) and the binary radix-tree nodes (uint32 x4:
- * left, right, first, last; bit 31 marks a leaf reference). */
+ * left, right, first, last; bit 31 marks a leaf reference; internal node i
+ * is the one that splits between sorted keys i and i + 1). */
 rt_status rt_debug_blas_scratch_layout(uint32_t n_tris, uint32_t flags, uint64_t *keys_off, uint64_t *ids_off,
                                        uint64_t *bin_off);
 

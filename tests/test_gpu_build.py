@@ -51,7 +51,28 @@ def test_invalid_width_rejected(ctx):
         assert e.value.code == rtcore.RT_ERR_INVALID_ARG
 
 
+def _radix_tree_canonical(bn):
+    """The radix tree of a (left, right, first, last) node array without its
+    numbering: per internal node its key range and each child's range (leaf
+    flag, first, last), sorted by range."""
+    bn = bn.astype(np.int64)
+    first, last = bn[:, 2], bn[:, 3]
+
+    def child(x):
+        leaf = (x & 0x80000000) != 0
+        idx = x & 0x7FFFFFFF
+        inner = np.where(leaf, 0, idx)
+        return np.stack([leaf.astype(np.int64), np.where(leaf, idx, first[inner]), np.where(leaf, idx, last[inner])], 1)
+
+    rows = np.concatenate([bn[:, 2:4], child(bn[:, 0]), child(bn[:, 1])], 1)
+    return rows[np.lexsort((rows[:, 1], rows[:, 0]))]
+
+
 def test_blas_stages_bit_exact(ctx, orc):
+    """Sorted keys and primitive ids byte for byte; the binary radix tree
+    node for node (the oracle numbers its nodes top-down, the GPU's
+    bottom-up build numbers internal node i by its split between keys i and
+    i + 1: the trees are compared by key ranges)."""
     import rtcore
     n = 50000
     items = soup(n, seed=5)
@@ -61,7 +82,13 @@ def test_blas_stages_bit_exact(ctx, orc):
     s = host(g.scratch)
     np.testing.assert_array_equal(s[koff:koff + 8 * n].view(np.uint64), ks)
     np.testing.assert_array_equal(s[ioff:ioff + 4 * n].view(np.uint32), ids)
-    np.testing.assert_array_equal(s[boff:boff + 16 * (n - 1)].view(np.uint32).reshape(-1, 4), bn)
+    gb = s[boff:boff + 16 * (n - 1)].view(np.uint32).reshape(-1, 4)
+    np.testing.assert_array_equal(_radix_tree_canonical(gb), _radix_tree_canonical(bn))
+    # internal node i splits between keys i and i + 1
+    left = gb[:, 0].astype(np.int64)
+    leaf = (left & 0x80000000) != 0
+    left_last = np.where(leaf, left & 0x7FFFFFFF, gb[np.where(leaf, 0, left), 3])
+    assert np.array_equal(left_last, np.arange(n - 1))
 
 
 def test_blas_duplicates_degenerates_and_bad_indices(ctx, orc):
