@@ -560,7 +560,7 @@ def run_ours(args) -> int:
                                  "achieved_gbs": round(N_TRIS * BYTES_BUILD_PER_TRI / (statistics.median(build_ms) * 1e-3) / 1e9, 1),
                                  "frac_of_hbm": round(N_TRIS * BYTES_BUILD_PER_TRI / (statistics.median(build_ms) * 1e-3) / 1e9
                                                       / peaks["hbm_gbs"], 4),
-                                 "note": "latency-bound: 14 dependent launches (eight sort passes), the collapse a cooperative grid of level barriers"},
+                                 "note": "latency-bound: 15 dependent launches (eight sort passes), the collapse a cooperative grid of level barriers"},
                              "wall_s_timed_region": round(t_wall, 3)},
                "secondary": extra,
                "clocks": clk}

@@ -158,9 +158,11 @@ __device__ __forceinline__ void block_minmax_atomic(int32_t *cbounds, const int3
 // Header / init
 // ---------------------------------------------------------------------------
 
-__global__ void k_init(rt_accel_header hdr, uint8_t *accel, int32_t *cbounds, GeomParams gp, uint32_t write_table) {
+__global__ void k_init(rt_accel_header hdr, uint8_t *accel, int32_t *cbounds, uint32_t *root, GeomParams gp,
+                       uint32_t write_table) {
     int t = threadIdx.x;
     if (t == 0) *reinterpret_cast<rt_accel_header *>(accel) = hdr;
+    if (t == 0) *root = kNone;  // the radix tree's root: none until k_tree completes it
     if (t < 3) { cbounds[t] = INT32_MAX; cbounds[3 + t] = INT32_MIN; }
     if (write_table) {
         uint32_t *tab = reinterpret_cast<uint32_t *>(accel + hdr.geom_offset);
@@ -439,6 +441,17 @@ __device__ __forceinline__ uint64_t exch_acq_rel(uint64_t *p, uint64_t v) {
     return old;
 }
 
+// The root k_tree completed: a completed root is reached only through nodes
+// completed in this build, every reference in range.  If keys left out of
+// order by a sort that gave up kept it from completing one, leaf 0 stands in
+// and RT_ERR_BOUNDS is recorded, so the collapse reads nothing out of range.
+__global__ void k_tree_root(uint32_t *root, uint32_t n, uint32_t *err) {
+    const uint32_t r = *root, i = r & ~kLeafBit;
+    if ((r & kLeafBit) ? i < n : i + 1u < n) return;
+    report_error(err, RT_ERR_BOUNDS, 0x66000000u | (i & 0xffffffu));
+    *root = kLeafBit;
+}
+
 __global__ void __launch_bounds__(256) k_tree(TreeArgs a) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = a.n;
@@ -447,7 +460,8 @@ __global__ void __launch_bounds__(256) k_tree(TreeArgs a) {
     const uint32_t id = __ldg(a.ids + j);
     uint64_t kl = __ldg(a.keys + j), kr = kl;
     uint64_t klm = j > 0 ? __ldg(a.keys + j - 1) : 0ull, krp = j + 1 < n ? __ldg(a.keys + j + 1) : 0ull;
-    const Box lb = load_box(a.boxes, id);
+    if (id >= n) report_error(a.err, RT_ERR_BOUNDS, 0x67000000u | (j & 0xffffffu));  // not a sorted id
+    const Box lb = id < n ? load_box(a.boxes, id) : box_empty();
     store_box(a.leaf_box, j, lb);
     if (n < 2) return;
     uint32_t me = kLeafBit | j, l = j, r = j;
@@ -1119,16 +1133,25 @@ __global__ void __launch_bounds__(kCollapseThreads, 4) k_collapse(CollapseArgs a
 
 // Leaf records in node order: record d is the input record of sorted
 // primitive gather[d] (written by the collapse's phase B).  One thread per
-// record; the grid covers every record.
+// record; the grid covers every record.  An index out of range (only an
+// incomplete tree leaves one) records RT_ERR_BOUNDS and a zero record.
 template <int RW>
 __global__ void __launch_bounds__(256) k_gather_records(const uint4 *__restrict__ recs_in, uint4 *__restrict__ recs_out,
                                                         const uint32_t *__restrict__ ids,
-                                                        const uint32_t *__restrict__ gather, uint32_t n) {
+                                                        const uint32_t *__restrict__ gather, uint32_t n, uint32_t *err) {
     const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
-    const uint4 *src = recs_in + (size_t)__ldg(ids + __ldg(gather + d)) * RW;
+    const uint32_t gi = __ldg(gather + d);
+    const uint32_t id = gi < n ? __ldg(ids + gi) : n;
     uint4 *dst = recs_out + (size_t)d * RW;
     uint4 r[RW];
+    if (id >= n) {
+        report_error(err, RT_ERR_BOUNDS, 0x68000000u | (d & 0xffffffu));
+#pragma unroll
+        for (int w = 0; w < RW; ++w) dst[w] = make_uint4(0u, 0u, 0u, 0u);
+        return;
+    }
+    const uint4 *src = recs_in + (size_t)id * RW;
 #pragma unroll
     for (int w = 0; w < RW; ++w) r[w] = __ldg(src + w);
 #pragma unroll
@@ -1198,7 +1221,8 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
 
     int32_t *cb = reinterpret_cast<int32_t *>(S + L.misc);
     static GeomParams empty_gp;  // zero-initialised; used by TLAS builds
-    k_init<<<1, 256, 0, st>>>(h, A, cb, gp ? *gp : empty_gp, gp ? 1u : 0u);
+    uint32_t *root_word = reinterpret_cast<uint32_t *>(S + L.misc + 64u);
+    k_init<<<1, 256, 0, st>>>(h, A, cb, root_word, gp ? *gp : empty_gp, gp ? 1u : 0u);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     uint32_t *hdr_status = reinterpret_cast<uint32_t *>(A) + 7;  // rt_accel_header::status
     if (n == 0) {
@@ -1234,7 +1258,6 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     if (sst) return set_error(ctx, sst, "radix sort launch failed");
 
     uint4 *bin = reinterpret_cast<uint4 *>(S + L.bin);
-    uint32_t *root_word = reinterpret_cast<uint32_t *>(S + L.misc + 64u);
     if (n >= 2) RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.visit, 0xff, (size_t)(n - 1) * 8u, st));
     TreeArgs ta;
     ta.n = n;
@@ -1250,6 +1273,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     ta.root = root_word;
     ta.err = ctx->d_err;
     k_tree<<<nb, 256, 0, st>>>(ta);
+    if (n >= 2) k_tree_root<<<1, 1, 0, st>>>(root_word, n, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
 
     CollapseArgs ca;
@@ -1285,9 +1309,9 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
                                                  dim3(kCollapseThreads), args, 0, st));
     uint4 *recs_out = reinterpret_cast<uint4 *>(A + h.prim_offset);
     if (bc.rec_bytes == 48u)
-        k_gather_records<3><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n);
+        k_gather_records<3><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n, ctx->d_err);
     else
-        k_gather_records<5><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n);
+        k_gather_records<5><<<nb, 256, 0, st>>>(recs, recs_out, ids0, ids1, n, ctx->d_err);
     RT_CUDA_CTX(ctx, cudaGetLastError());
     return RT_OK;
 }
