@@ -44,7 +44,7 @@ struct GeomParams {
 };
 
 struct BuildLayout {
-    uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, node_box, node_cost, leafable, visit, leaf_box,
+    uint64_t recs, boxes, keys0, keys1, ids0, ids1, bin, node_box, node_cost, leafable, other, leaf_box,
         wq, slots, desc, counts, blk, misc, sort, total;
 };
 
@@ -77,7 +77,7 @@ BuildLayout build_layout(uint32_t n, uint32_t rec_bytes, int passes) {
     L.node_box = take(ni * 32u);
     L.node_cost = take(ni * 4u);
     L.leafable = take(ni);
-    L.visit = take(ni * 8u);
+    L.other = take(ni * 8u);  // k_tree: per internal node, the first child's reference and far end
     L.leaf_box = take((uint64_t)n * 32u);
     L.wq = take(cap * 4u);
     L.slots = take(cap * 32u);
@@ -1261,7 +1261,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     if (sst) return set_error(ctx, sst, "radix sort launch failed");
 
     uint4 *bin = reinterpret_cast<uint4 *>(S + L.bin);
-    if (n >= 2) RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.visit, 0xff, (size_t)(n - 1) * 8u, st));
+    if (n >= 2) RT_CUDA_CTX(ctx, cudaMemsetAsync(S + L.other, 0xff, (size_t)(n - 1) * 8u, st));
     TreeArgs ta;
     ta.n = n;
     ta.keys = keys0;
@@ -1271,7 +1271,7 @@ int run_build(rt_context *ctx, cudaStream_t st, const BuildCall &bc, const GeomP
     ta.node_box = reinterpret_cast<float *>(S + L.node_box);
     ta.node_cost = reinterpret_cast<float *>(S + L.node_cost);
     ta.leafable = reinterpret_cast<uint8_t *>(S + L.leafable);
-    ta.other = reinterpret_cast<uint64_t *>(S + L.visit);
+    ta.other = reinterpret_cast<uint64_t *>(S + L.other);
     ta.leaf_box = reinterpret_cast<float *>(S + L.leaf_box);
     ta.root = root_word;
     ta.err = ctx->d_err;
