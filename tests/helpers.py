@@ -233,3 +233,20 @@ def single_instance(blas_ref: int) -> np.ndarray:
 
 def ptr_of(a: np.ndarray) -> int:
     return a.ctypes.data_as(C.c_void_p).value
+
+
+def radix_tree_canonical(bn):
+    """The radix tree of a (left, right, first, last) node array without its
+    numbering: per internal node its key range and each child's range (leaf
+    flag, first, last), sorted by range."""
+    bn = bn.astype(np.int64)
+    first, last = bn[:, 2], bn[:, 3]
+
+    def child(x):
+        leaf = (x & 0x80000000) != 0
+        idx = x & 0x7FFFFFFF
+        inner = np.where(leaf, 0, idx)
+        return np.stack([leaf.astype(np.int64), np.where(leaf, idx, first[inner]), np.where(leaf, idx, last[inner])], 1)
+
+    rows = np.concatenate([bn[:, 2:4], child(bn[:, 0]), child(bn[:, 1])], 1)
+    return rows[np.lexsort((rows[:, 1], rows[:, 0]))]

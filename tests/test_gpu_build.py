@@ -6,7 +6,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from helpers import GpuBlas, GpuTlas, compare_accels, dev, header, host, ref8_instances, ref8_items, ptr_of
+from helpers import (GpuBlas, GpuTlas, compare_accels, dev, header, host, ptr_of, radix_tree_canonical, ref8_instances,
+                     ref8_items)
 
 pytestmark = pytest.mark.gpu
 
@@ -51,23 +52,6 @@ def test_invalid_width_rejected(ctx):
         assert e.value.code == rtcore.RT_ERR_INVALID_ARG
 
 
-def _radix_tree_canonical(bn):
-    """The radix tree of a (left, right, first, last) node array without its
-    numbering: per internal node its key range and each child's range (leaf
-    flag, first, last), sorted by range."""
-    bn = bn.astype(np.int64)
-    first, last = bn[:, 2], bn[:, 3]
-
-    def child(x):
-        leaf = (x & 0x80000000) != 0
-        idx = x & 0x7FFFFFFF
-        inner = np.where(leaf, 0, idx)
-        return np.stack([leaf.astype(np.int64), np.where(leaf, idx, first[inner]), np.where(leaf, idx, last[inner])], 1)
-
-    rows = np.concatenate([bn[:, 2:4], child(bn[:, 0]), child(bn[:, 1])], 1)
-    return rows[np.lexsort((rows[:, 1], rows[:, 0]))]
-
-
 def test_blas_stages_bit_exact(ctx, orc):
     """Sorted keys and primitive ids byte for byte; the binary radix tree
     node for node (the oracle numbers its nodes top-down, the GPU's
@@ -83,7 +67,7 @@ def test_blas_stages_bit_exact(ctx, orc):
     np.testing.assert_array_equal(s[koff:koff + 8 * n].view(np.uint64), ks)
     np.testing.assert_array_equal(s[ioff:ioff + 4 * n].view(np.uint32), ids)
     gb = s[boff:boff + 16 * (n - 1)].view(np.uint32).reshape(-1, 4)
-    np.testing.assert_array_equal(_radix_tree_canonical(gb), _radix_tree_canonical(bn))
+    np.testing.assert_array_equal(radix_tree_canonical(gb), radix_tree_canonical(bn))
     # internal node i splits between keys i and i + 1
     left = gb[:, 0].astype(np.int64)
     leaf = (left & 0x80000000) != 0
