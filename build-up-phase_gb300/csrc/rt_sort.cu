@@ -26,11 +26,13 @@ namespace {
 
 constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
-// 16 keys per thread: tiles of 8,192 keys, half as many tiles for the
-// look-back's wave to cross (one 112 KB block per SM; 1M-key soup build
-// 0.807 -> 0.792 ms against 8 keys per thread, same bytes)
-constexpr int kSortItems = 16;
+// 14 keys per thread: tiles of 7,168 keys, 140 tiles for 1M keys, one wave
+// of one 98 KB block per SM on 152 SMs (8 keys per thread: 245 tiles, two
+// waves, 1M-key soup build 0.807 ms; 16: 123 tiles, 0.792 ms then and equal
+// to 14 now on the soup; 14: 2M box 1.317 -> 1.306 ms)
+constexpr int kSortItems = 14;
 constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRankGroup = 8;  // keys ranked together (their votes, atomics and shuffles back to back)
 constexpr int kRadix = 256;
 // Statuses read per look-back round trip.  Tiles of one wave publish their
 // aggregates at about the same time, so a walk of one predecessor per round
@@ -135,11 +137,12 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
     // (applied in issue order, which keeps the ranks in input order), then
     // the shuffles of the old counts, so no key waits on the one before it.
 #pragma unroll
-    for (int j0 = 0; j0 < kSortItems; j0 += 8) {
-        uint32_t pm[8], old[8];
+    for (int j0 = 0; j0 < kSortItems; j0 += kRankGroup) {
+        uint32_t pm[kRankGroup], old[kRankGroup];
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
+        for (int jj = 0; jj < kRankGroup; ++jj) {
             const int j = j0 + jj;
+            if (j >= kSortItems) break;  // a last, shorter group
             const uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
             uint32_t peers = __ballot_sync(0xffffffffu, wbase + (uint32_t)j * 32u + (uint32_t)lane < n);
 #pragma unroll
@@ -150,16 +153,20 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint64_t *__res
             pm[jj] = peers;
         }
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-            const uint32_t d = (uint32_t)(k[j0 + jj] >> shift) & dmask;
+        for (int jj = 0; jj < kRankGroup; ++jj) {
+            const int j = j0 + jj;
+            if (j >= kSortItems) break;
+            const uint32_t d = (uint32_t)(k[j] >> shift) & dmask;
             old[jj] = 0u;
             if ((int)(__ffs(pm[jj]) - 1) == lane)
                 old[jj] = atomicAdd(&s_whist[w * kRadix + d], (uint32_t)__popc(pm[jj]));
         }
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
+        for (int jj = 0; jj < kRankGroup; ++jj) {
+            const int j = j0 + jj;
+            if (j >= kSortItems) break;
             const int leader = pm[jj] ? __ffs(pm[jj]) - 1 : lane;
-            rank[j0 + jj] = __shfl_sync(0xffffffffu, old[jj], leader) + (uint32_t)__popc(pm[jj] & lt);
+            rank[j] = __shfl_sync(0xffffffffu, old[jj], leader) + (uint32_t)__popc(pm[jj] & lt);
         }
     }
     __syncthreads();
