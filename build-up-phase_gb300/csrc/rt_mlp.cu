@@ -174,6 +174,17 @@ constexpr int kQueryRows = 128;
 // per weight and tile), then delta_{L-1} = (delta_L W_L) * relu'(A_{L-1})
 // with W_L read transposed by ldmatrix.trans from its forward layout.
 
+// Programmatic dependent launch between the training kernels (forward +
+// backward, Adam, the next batch's forward + backward): each kernel lets the
+// next one launch as soon as all of its own blocks run, then waits for the
+// kernel before it to complete (its writes visible) before it reads or
+// writes anything, so a launch's scheduling overlaps the previous kernel's
+// tail.  Launched without the attribute both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 constexpr int kTrainRows = 128;
 constexpr int kTrainThreads = 256;
 __host__ __device__ constexpr int tw_rows(int l) { return l == 5 ? 16 : 64; }  // weight rows kept in shared memory
@@ -350,6 +361,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_cache_fwd_bwd(CacheState *
                                                                     const float4 *targets, uint32_t n,
                                                                     float inv_count, const uint32_t *n_dev,
                                                                     uint32_t row0, uint32_t bump_step) {
+    pdl_enter();
     if (bump_step && blockIdx.x == 0 && threadIdx.x == 0) S->step += 1u;
     if (n_dev) {
         // rows [row0, row0 + n) of a set whose size is produced on the device
@@ -795,6 +807,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cache_query_tc(const CacheSta
 // the k_cache_fwd_bwd launch before).  Thread 0 also hands the batch's mean
 // loss to loss_out and clears it for the next batch.
 __global__ void k_cache_adam(CacheState *S, float *loss_out) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         if (loss_out) *loss_out = S->loss;
@@ -820,6 +833,23 @@ __global__ void k_cache_refresh_bf16(CacheState *S) {
     if (i < kParams) S->wbf[i] = __float2bfloat16(S->params[i]);
 }
 
+// Launch with programmatic stream serialization (see pdl_enter).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned threads, size_t smem, cudaStream_t st,
+                       Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 int set_smem(rt_context *ctx) {
     RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_query_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
     RT_CUDA_CTX(ctx, cudaFuncSetAttribute(k_cache_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
@@ -832,9 +862,9 @@ int launch_fwd_bwd(rt_context *ctx, cudaStream_t st, CacheState *S, const rt_cac
     uint32_t grid = (uint32_t)ctx->sm_count;
     if (grid > tiles) grid = tiles;
     if (grid == 0) return RT_OK;
-    k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(tg), n,
-                                                   1.0f / (3.0f * (float)n), nullptr, 0u, bump_step);
-    RT_CUDA_CTX(ctx, cudaGetLastError());
+    RT_CUDA_CTX(ctx, launch_pdl(k_cache_fwd_bwd, grid, kTrainThreads, kTrainSmem, st, S, in,
+                                reinterpret_cast<const float4 *>(tg), n, 1.0f / (3.0f * (float)n),
+                                static_cast<const uint32_t *>(nullptr), 0u, bump_step));
     return RT_OK;
 }
 
@@ -930,8 +960,7 @@ extern "C" rt_status rt_cache_train(rt_context *ctx, rt_stream stream, void *cac
         const uint32_t m = (n - b) < batch ? (n - b) : batch;
         rc = launch_fwd_bwd(ctx, st, S, in + b, targets + 4u * (size_t)b, m, 1u);
         if (rc) return rc;
-        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S, loss_out);
-        RT_CUDA_CTX(ctx, cudaGetLastError());
+        RT_CUDA_CTX(ctx, launch_pdl(k_cache_adam, (kParams + 255) / 256, 256, 0, st, S, loss_out));
     }
     return RT_OK;
 }
@@ -1081,10 +1110,10 @@ int cache_train_dev(rt_context *ctx, cudaStream_t st, void *cache, const rt_cach
         const uint32_t tiles = (m + kTrainRows - 1) / kTrainRows;
         uint32_t grid = (uint32_t)ctx->sm_count;
         if (grid > tiles) grid = tiles;
-        k_cache_fwd_bwd<<<grid, kTrainThreads, kTrainSmem, st>>>(S, in, reinterpret_cast<const float4 *>(targets), m, 0.0f,
-                                                       n_dev, b, 1u);
-        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(S, nullptr);
-        RT_CUDA_CTX(ctx, cudaGetLastError());
+        RT_CUDA_CTX(ctx, launch_pdl(k_cache_fwd_bwd, grid, kTrainThreads, kTrainSmem, st, S, in,
+                                    reinterpret_cast<const float4 *>(targets), m, 0.0f, n_dev, b, 1u));
+        RT_CUDA_CTX(ctx, launch_pdl(k_cache_adam, (kParams + 255) / 256, 256, 0, st, S,
+                                    static_cast<float *>(nullptr)));
     }
     return RT_OK;
 }
